@@ -1,0 +1,350 @@
+"""Benchmark: clause x assignment checks/s of the GB300 check pass.
+
+Workload (one "step" = one pass): the plain check at scale - 2^20 variables,
+4e6 clauses with lengths 2..100 (60% uniform on 2..16, 40% geometric tail),
+1024 partial assignments from 32 solvers (32 each) assigning 40-90% of the
+variables with fair signs, 0.1% planted reports; seeded synthetic data of
+those shapes (the reference publishes no dataset).
+
+value: checks/s with the clause database and the assignment planes resident
+       in HBM (kernel passes back to back, CUDA events on the launch stream).
+e2e:   the same metric through the C ABI call gss_check_pass_host with host
+       buffers: per step the assignment planes go host->device from pinned
+       memory and the reports come back device->host.
+The inputs (about 0.6 GB) are larger than the 129 MB L2, so no flush is
+needed between steps.
+
+--impl reference times the CPU restatement of the reference's check (the
+reference has no CPU implementation of its own and its CUDA build cannot run
+on the benchmark host) on all host cores, on a bounded sample of the same
+workload.
+
+Multi-GPU: clauses are independent, so with N ranks each rank checks its own
+database shard of the same size (weak scaling) with no collective on the
+data path; value = all ranks' checks / the slowest rank's time.
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "clause x assignment checks/s (bit-exact, plain check at scale)"
+UNIT = "checks/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--clauses", type=int, default=4_000_000)
+    p.add_argument("--vars-log2", type=int, default=20)
+    p.add_argument("--e2e-steps", type=int, default=5)
+    p.add_argument("--cpu-seconds", type=float, default=15.0)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def config_dict(args, world):
+    return {
+        "workload": "plain check at scale: %d clauses (lengths 2-100) x 1024 assignments (32 solvers x 32), "
+                    "2^%d variables, 0.1%% planted reports" % (args.clauses, args.vars_log2),
+        "clauses_per_gpu": args.clauses,
+        "assignments": 1024,
+        "variables": 2 ** args.vars_log2,
+        "solvers": 32,
+        "l2": "inputs larger than L2 (no flush)",
+        "parallelism": "clause shards, %d replica(s)" % world,
+    }
+
+
+def algorithmic_bytes(wl, n_reports):
+    """4*sum(L) + 8*V*ceil(A/32) + 16*R per pass."""
+    words = (wl.n_assignments + 31) // 32
+    return 4 * wl.n_lits + 8 * wl.n_vars * words + 16 * n_reports
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def load_traffic():
+    """Per-launch DRAM bytes of the check kernel from the committed ncu summary
+    (scaled to this workload there), or None."""
+    path = os.path.join(ROOT, "profiles", "check_kernel_traffic.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f).get("dram_bytes_per_launch")
+    return None
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm = [float(r[1]) for r in self.rows if len(r) >= 9 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) >= 9 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            if len(r) >= 9:
+                for i, n in enumerate(names):
+                    if r[5 + i].lower() == "active":
+                        reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_workload(args, rank):
+    from gpusharesat_gb300 import workloads as W
+    return W.make_scale(seed=1 + 1000 * rank, n_vars=2 ** args.vars_log2, n_clauses=args.clauses)
+
+
+def cpu_baseline(wl, seconds, threads=None):
+    """Times the oracle (C restatement, all host cores) on a prefix of the
+    clause database sized to take about `seconds`. Returns checks/s and the
+    sample description."""
+    import oracle
+    threads = threads or os.cpu_count() or 1
+    n = min(wl.n_clauses, 20000)
+    while True:
+        t0 = time.perf_counter()
+        oracle.check(wl.lits, wl.offsets[:n + 1], wl.state, wl.start, n_threads=threads)
+        dt = time.perf_counter() - t0
+        if dt >= seconds / 4 or n >= wl.n_clauses:
+            break
+        n = min(wl.n_clauses, int(n * max(2.0, (seconds / 4) / max(dt, 1e-3))))
+    reps = max(1, int(seconds / max(dt, 1e-3)))
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        oracle.check(wl.lits, wl.offsets[:n + 1], wl.state, wl.start, n_threads=threads)
+    dt = (time.perf_counter() - t0) / reps
+    return n * wl.n_assignments / dt, threads, "%d of %d clauses x %d assignments, %d rep(s)" % (
+        n, wl.n_clauses, wl.n_assignments, reps)
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import oracle
+    oracle.build()
+    wl = make_workload(args, 0)
+    threads = os.cpu_count() or 1
+    # size one step's sample to about 2 s of CPU work
+    n = 20000
+    t0 = time.perf_counter()
+    oracle.check(wl.lits, wl.offsets[:n + 1], wl.state, wl.start, n_threads=threads)
+    dt = time.perf_counter() - t0
+    n = int(min(wl.n_clauses, max(n, n * 2.0 / max(dt, 1e-3))))
+    for _ in range(args.warmup):
+        oracle.check(wl.lits, wl.offsets[:n + 1], wl.state, wl.start, n_threads=threads)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        oracle.check(wl.lits, wl.offsets[:n + 1], wl.state, wl.start, n_threads=threads)
+        times.append(time.perf_counter() - t0)
+    per_step = float(np.mean(times))
+    value = n * wl.n_assignments / per_step
+    sample = "%d of %d clauses x %d assignments per step" % (n, wl.n_clauses, wl.n_assignments)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_step * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded)",
+        "config": config_dict(args, world),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "CPU restatement of the reference's check rule (the reference has no CPU path; its CUDA build "
+                "cannot run here), all host threads",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args):
+    import torch
+    import torch.distributed as dist
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    import gpusharesat_gb300 as g
+    from gpusharesat_gb300 import build as b
+    b.build()
+
+    wl = make_workload(args, rank)
+    stream = torch.cuda.Stream()
+    eng = g.Engine(local)
+    eng.set_stream(stream.cuda_stream)
+    eng.set_db(wl.lits, wl.offsets)
+    eng.set_state(wl.state, wl.start, wl.solver_of_word)
+    # size the queues: run once (grows on overflow)
+    rep = eng.check()
+    n_reports = len(rep)
+    del rep
+
+    # ---- device-resident timing (value) ----
+    for _ in range(args.warmup):
+        eng.launch()
+    torch.cuda.synchronize()
+    eng.kernel_time()  # drop warm-up events
+    eng.set_timing(True)
+    sampler = ClockSampler(local) if rank == 0 else None
+    barrier()
+    torch.cuda.synchronize()
+    if sampler:
+        sampler.start()
+        time.sleep(0.3)
+    launches0 = eng.launch_count
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        eng.launch()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clocks = sampler.stop() if sampler else None
+    gpu_launches = eng.launch_count - launches0
+    eng.set_timing(False)
+    n_last = eng.wait()
+    assert n_last == n_reports, (n_last, n_reports)
+    elapsed_ms = ev0.elapsed_time(ev1)
+    kern_ms, kern_n = eng.kernel_time()
+    t = torch.tensor([elapsed_ms], device="cuda")
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    elapsed_ms = float(t.item())
+    ms_per_step = elapsed_ms / args.steps
+    checks_per_pass = wl.n_clauses * wl.n_assignments
+    value = checks_per_pass * world / (ms_per_step / 1e3)
+
+    # ---- end to end through host buffers (e2e) ----
+    state_h = torch.from_numpy(wl.state.reshape(-1)).pin_memory()
+    start_h = torch.from_numpy(wl.start).pin_memory()
+    sow_h = torch.from_numpy(wl.solver_of_word).pin_memory()
+    out_h = torch.empty((n_reports + 1024) * 4, dtype=torch.int32).pin_memory()
+    lib = g.load()
+    nrep = ctypes.c_int64()
+
+    def e2e_step():
+        rc = lib.gss_check_pass_host(eng.h, ctypes.c_void_p(state_h.data_ptr()), wl.n_vars, wl.n_words,
+                                     ctypes.c_void_p(start_h.data_ptr()), ctypes.c_void_p(sow_h.data_ptr()),
+                                     ctypes.c_void_p(out_h.data_ptr()), n_reports + 1024, ctypes.byref(nrep))
+        g._check(rc)
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / args.e2e_steps
+    te = torch.tensor([e2e_s], device="cuda")
+    if world > 1:
+        dist.all_reduce(te, op=dist.ReduceOp.MAX)
+    e2e_s = float(te.item())
+    assert nrep.value == n_reports
+    h2d = wl.state.nbytes + wl.start.nbytes + wl.solver_of_word.nbytes
+    d2h = n_reports * 16 + 16 * 4
+
+    if rank == 0:
+        peak, peak_kind = load_peaks()
+        kern_avg_s = (kern_ms / max(kern_n, 1)) / 1e3
+        B = algorithmic_bytes(wl, n_reports)
+        achieved = B / kern_avg_s / 1e9
+        roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                    "frac": achieved / peak, "traffic": load_traffic(),
+                    "algorithmic_bytes_per_launch": B, "kernel_ms": kern_avg_s * 1e3,
+                    "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+                    else "fallback"}
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded)",
+            "config": config_dict(args, world),
+            "reports_per_pass": n_reports,
+            "e2e": {"value": checks_per_pass * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3},
+            "roofline": roofline,
+            "gpu_launches": gpu_launches,
+            "clocks": clocks,
+        }
+        if not args.no_cpu_baseline:
+            v, cores, sample = cpu_baseline(wl, args.cpu_seconds)
+            line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+        print(json.dumps(line), flush=True)
+    eng.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,399 @@
+// The engine: device-resident clause database, assignment bit planes and
+// report queues, and the C ABI of include/gpusharesat.h (engine layer).
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <mutex>
+#include <vector>
+
+#include "common.h"
+
+namespace gss {
+
+static thread_local std::string g_last_error = "no error";
+
+int set_error(int code, const char *fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+int DevBuf::reserve(size_t need) {
+    if (need <= bytes && ptr) return GSS_OK;
+    release();
+    size_t cap = 256;
+    while (cap < need) cap *= 2;
+    cudaError_t e = cudaMalloc(&ptr, cap);
+    if (e != cudaSuccess) {
+        ptr = nullptr;
+        cudaGetLastError();
+        return set_error(GSS_ERR_NOMEM, "cudaMalloc(%zu) failed: %s", cap, cudaGetErrorString(e));
+    }
+    bytes = cap;
+    return GSS_OK;
+}
+
+int DevBuf::grow_keep(size_t need, cudaStream_t stream, size_t keep_bytes) {
+    if (need <= bytes && ptr) return GSS_OK;
+    size_t cap = bytes ? bytes : 256;
+    while (cap < need) cap *= 2;
+    void *np = nullptr;
+    cudaError_t e = cudaMalloc(&np, cap);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(GSS_ERR_NOMEM, "cudaMalloc(%zu) failed: %s", cap, cudaGetErrorString(e));
+    }
+    if (ptr && keep_bytes) {
+        GSS_CUDA_TRY(cudaMemcpyAsync(np, ptr, keep_bytes, cudaMemcpyDeviceToDevice, stream));
+        GSS_CUDA_TRY(cudaStreamSynchronize(stream));
+    }
+    release();
+    ptr = np;
+    bytes = cap;
+    return GSS_OK;
+}
+
+void DevBuf::release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+}
+
+int PinnedBuf::reserve(size_t need) {
+    if (need <= bytes && ptr) return GSS_OK;
+    release();
+    size_t cap = 4096;
+    while (cap < need) cap *= 2;
+    cudaError_t e = cudaMallocHost(&ptr, cap);
+    if (e != cudaSuccess) {
+        ptr = nullptr;
+        cudaGetLastError();
+        return set_error(GSS_ERR_NOMEM, "cudaMallocHost(%zu) failed: %s", cap, cudaGetErrorString(e));
+    }
+    bytes = cap;
+    return GSS_OK;
+}
+
+void PinnedBuf::release() {
+    if (ptr) cudaFreeHost(ptr);
+    ptr = nullptr;
+    bytes = 0;
+}
+
+}  // namespace gss
+
+using namespace gss;
+
+struct gss_engine {
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    int64_t launches = 0;
+
+    // clause database (CSR)
+    DevBuf lits, offsets;
+    int64_t n_clauses = 0, n_lits = 0, max_var = -1;
+
+    // assignment state
+    DevBuf state, start, solver_of_word;
+    int64_t n_vars = 0;
+    int n_words = 0;
+
+    // report queues: n_parts partitions of cap_per_part records
+    DevBuf reports, counts;
+    uint32_t n_parts = 16;
+    uint32_t cap_per_part = 0;
+    int64_t requested_cap = 0;
+    PinnedBuf h_counts;
+    bool pass_pending = false;
+
+    // optional CUDA-event timing of each check kernel (on the launch stream)
+    bool timing = false;
+    std::vector<cudaEvent_t> ev_pool;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_pending;
+};
+
+namespace {
+
+int ensure_device(gss_engine *eng) {
+    GSS_CUDA_TRY(cudaSetDevice(eng->device));
+    return GSS_OK;
+}
+
+int ensure_queues(gss_engine *eng) {
+    int64_t want = eng->requested_cap;
+    if (want <= 0) {
+        // Automatic: room for a report per clause and word-block, at least 1M.
+        int64_t wb = (eng->n_words + 31) / 32;
+        want = std::max<int64_t>(int64_t(1) << 20, eng->n_clauses * std::max<int64_t>(wb, 1) * 2);
+    }
+    int64_t per = (want + eng->n_parts - 1) / eng->n_parts;
+    if (per > 0x7FFFFFFF) per = 0x7FFFFFFF;
+    if ((uint32_t) per > eng->cap_per_part || !eng->reports.ptr) {
+        GSS_TRY(eng->reports.reserve((size_t) per * eng->n_parts * sizeof(gss_report)));
+        eng->cap_per_part = (uint32_t) per;
+    }
+    GSS_TRY(eng->counts.reserve(sizeof(uint32_t) * eng->n_parts));
+    GSS_TRY(eng->h_counts.reserve(sizeof(uint32_t) * eng->n_parts));
+    return GSS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *gss_last_error(void) { return g_last_error.c_str(); }
+
+const char *gss_version(void) { return "gpusharesat-gb300 0.1 sm_103a"; }
+
+int gss_max_clause_len(void) { return kMaxClauseLen; }
+
+int gss_engine_create(int device, gss_engine **out) {
+    if (!out) return set_error(GSS_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    int n = 0;
+    GSS_CUDA_TRY(cudaGetDeviceCount(&n));
+    if (device < 0 || device >= n) return set_error(GSS_ERR_INVALID, "device %d out of range (%d devices)", device, n);
+    gss_engine *eng = new gss_engine();
+    eng->device = device;
+    int rc = ensure_device(eng);
+    if (rc == GSS_OK) {
+        cudaError_t e = cudaDeviceGetAttribute(&eng->sm_count, cudaDevAttrMultiProcessorCount, device);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&eng->own_stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) rc = set_error(GSS_ERR_CUDA, "engine setup failed: %s", cudaGetErrorString(e));
+    }
+    if (rc != GSS_OK) {
+        delete eng;
+        return rc;
+    }
+    eng->stream = eng->own_stream;
+    *out = eng;
+    return GSS_OK;
+}
+
+int gss_engine_destroy(gss_engine *eng) {
+    if (!eng) return GSS_OK;
+    cudaSetDevice(eng->device);
+    if (eng->stream) cudaStreamSynchronize(eng->stream);
+    if (eng->own_stream) cudaStreamDestroy(eng->own_stream);
+    for (auto &p : eng->ev_pending) {
+        cudaEventDestroy(p.first);
+        cudaEventDestroy(p.second);
+    }
+    for (auto e : eng->ev_pool) cudaEventDestroy(e);
+    delete eng;
+    return GSS_OK;
+}
+
+int gss_engine_set_stream(gss_engine *eng, void *stream) {
+    if (!eng) return set_error(GSS_ERR_INVALID, "engine is NULL");
+    eng->stream = stream ? (cudaStream_t) stream : eng->own_stream;
+    return GSS_OK;
+}
+
+int64_t gss_engine_launch_count(const gss_engine *eng) { return eng ? eng->launches : -1; }
+
+int gss_engine_set_timing(gss_engine *eng, int on) {
+    if (!eng) return set_error(GSS_ERR_INVALID, "engine is NULL");
+    eng->timing = on != 0;
+    return GSS_OK;
+}
+
+int gss_engine_kernel_time(gss_engine *eng, double *total_ms, int64_t *n_launches) {
+    if (!eng || !total_ms || !n_launches) return set_error(GSS_ERR_INVALID, "bad arguments to gss_engine_kernel_time");
+    GSS_TRY(ensure_device(eng));
+    double t = 0;
+    int64_t n = 0;
+    for (auto &p : eng->ev_pending) {
+        GSS_CUDA_TRY(cudaEventSynchronize(p.second));
+        float ms = 0;
+        GSS_CUDA_TRY(cudaEventElapsedTime(&ms, p.first, p.second));
+        t += ms;
+        n++;
+        eng->ev_pool.push_back(p.first);
+        eng->ev_pool.push_back(p.second);
+    }
+    eng->ev_pending.clear();
+    *total_ms = t;
+    *n_launches = n;
+    return GSS_OK;
+}
+
+int gss_db_set(gss_engine *eng, const int32_t *lits, const int64_t *offsets, int64_t n_clauses) {
+    if (!eng || !offsets || n_clauses < 0) return set_error(GSS_ERR_INVALID, "bad arguments to gss_db_set");
+    if (n_clauses > 0xFFFFFFF0LL) return set_error(GSS_ERR_INVALID, "too many clauses (%lld)", (long long) n_clauses);
+    if (offsets[0] != 0) return set_error(GSS_ERR_INVALID, "offsets[0] must be 0");
+    int64_t max_var = -1;
+    for (int64_t c = 0; c < n_clauses; c++) {
+        int64_t len = offsets[c + 1] - offsets[c];
+        if (len < 1 || len > kMaxClauseLen)
+            return set_error(GSS_ERR_INVALID, "clause %lld has length %lld (allowed 1..%d)", (long long) c,
+                             (long long) len, kMaxClauseLen);
+    }
+    const int64_t n_lits = offsets[n_clauses];
+    if (n_lits > 0 && !lits) return set_error(GSS_ERR_INVALID, "lits is NULL");
+    for (int64_t i = 0; i < n_lits; i++) {
+        if (lits[i] < 0) return set_error(GSS_ERR_INVALID, "literal %lld is negative", (long long) i);
+        int64_t v = lits[i] >> 1;
+        if (v > max_var) max_var = v;
+    }
+    GSS_TRY(ensure_device(eng));
+    GSS_CUDA_TRY(cudaStreamSynchronize(eng->stream));
+    GSS_TRY(eng->lits.reserve(std::max<int64_t>(n_lits, 1) * sizeof(int32_t)));
+    GSS_TRY(eng->offsets.reserve((n_clauses + 1) * sizeof(int64_t)));
+    if (n_lits) GSS_CUDA_TRY(cudaMemcpy(eng->lits.ptr, lits, n_lits * sizeof(int32_t), cudaMemcpyHostToDevice));
+    GSS_CUDA_TRY(cudaMemcpy(eng->offsets.ptr, offsets, (n_clauses + 1) * sizeof(int64_t), cudaMemcpyHostToDevice));
+    eng->n_clauses = n_clauses;
+    eng->n_lits = n_lits;
+    eng->max_var = max_var;
+    return GSS_OK;
+}
+
+int64_t gss_db_clause_count(const gss_engine *eng) { return eng ? eng->n_clauses : -1; }
+int64_t gss_db_literal_count(const gss_engine *eng) { return eng ? eng->n_lits : -1; }
+int64_t gss_db_max_var(const gss_engine *eng) { return eng ? eng->max_var : -1; }
+
+int gss_state_set(gss_engine *eng, const uint32_t *state, int64_t n_vars, int n_words, const uint32_t *start,
+                  const int32_t *solver_of_word, int on_device) {
+    if (!eng || n_vars < 0 || n_words < 0 || (n_vars > 0 && n_words > 0 && !state) || (n_words > 0 && !start))
+        return set_error(GSS_ERR_INVALID, "bad arguments to gss_state_set");
+    if (n_words > 4096) return set_error(GSS_ERR_INVALID, "at most 4096 words (131072 slots) per pass");
+    GSS_TRY(ensure_device(eng));
+    const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    const size_t sbytes = (size_t) n_vars * n_words * 2 * sizeof(uint32_t);
+    if (eng->pass_pending) GSS_CUDA_TRY(cudaStreamSynchronize(eng->stream));
+    GSS_TRY(eng->state.reserve(std::max<size_t>(sbytes, 8)));
+    GSS_TRY(eng->start.reserve(std::max<size_t>(n_words * sizeof(uint32_t), 4)));
+    GSS_TRY(eng->solver_of_word.reserve(std::max<size_t>(n_words * sizeof(int32_t), 4)));
+    if (sbytes) GSS_CUDA_TRY(cudaMemcpyAsync(eng->state.ptr, state, sbytes, kind, eng->stream));
+    if (n_words) {
+        GSS_CUDA_TRY(cudaMemcpyAsync(eng->start.ptr, start, n_words * sizeof(uint32_t), kind, eng->stream));
+        if (solver_of_word) {
+            GSS_CUDA_TRY(cudaMemcpyAsync(eng->solver_of_word.ptr, solver_of_word, n_words * sizeof(int32_t), kind,
+                                         eng->stream));
+        } else {
+            std::vector<int32_t> ident(n_words);
+            for (int w = 0; w < n_words; w++) ident[w] = w;
+            GSS_CUDA_TRY(cudaMemcpyAsync(eng->solver_of_word.ptr, ident.data(), n_words * sizeof(int32_t),
+                                         cudaMemcpyHostToDevice, eng->stream));
+            GSS_CUDA_TRY(cudaStreamSynchronize(eng->stream));
+        }
+    }
+    eng->n_vars = n_vars;
+    eng->n_words = n_words;
+    return GSS_OK;
+}
+
+int gss_check_set_capacity(gss_engine *eng, int64_t records) {
+    if (!eng || records < 0) return set_error(GSS_ERR_INVALID, "bad arguments to gss_check_set_capacity");
+    eng->requested_cap = records;
+    return GSS_OK;
+}
+
+int gss_check_launch(gss_engine *eng) {
+    if (!eng) return set_error(GSS_ERR_INVALID, "engine is NULL");
+    if (eng->n_clauses > 0 && eng->max_var >= eng->n_vars)
+        return set_error(GSS_ERR_INVALID, "database uses variable %lld but the state has %lld variables",
+                         (long long) eng->max_var, (long long) eng->n_vars);
+    GSS_TRY(ensure_device(eng));
+    GSS_TRY(ensure_queues(eng));
+    CheckArgs a;
+    a.lits = (const int32_t *) eng->lits.ptr;
+    a.offsets = (const int64_t *) eng->offsets.ptr;
+    a.n_clauses = (uint32_t) eng->n_clauses;
+    a.state = (const uint2 *) eng->state.ptr;
+    a.n_words = (uint32_t) eng->n_words;
+    a.start = (const uint32_t *) eng->start.ptr;
+    a.solver_of_word = (const int32_t *) eng->solver_of_word.ptr;
+    a.out = (gss_report *) eng->reports.ptr;
+    a.counts = (uint32_t *) eng->counts.ptr;
+    a.n_parts = eng->n_parts;
+    a.cap_per_part = eng->cap_per_part;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    if (eng->timing) {
+        for (cudaEvent_t *ev : {&ev0, &ev1}) {
+            if (!eng->ev_pool.empty()) {
+                *ev = eng->ev_pool.back();
+                eng->ev_pool.pop_back();
+            } else {
+                GSS_CUDA_TRY(cudaEventCreate(ev));
+            }
+        }
+    }
+    GSS_CUDA_TRY(cudaMemsetAsync(a.counts, 0, sizeof(uint32_t) * a.n_parts, eng->stream));
+    if (ev0) GSS_CUDA_TRY(cudaEventRecord(ev0, eng->stream));
+    GSS_TRY(launch_check(a, eng->stream, eng->sm_count));
+    if (ev1) {
+        GSS_CUDA_TRY(cudaEventRecord(ev1, eng->stream));
+        eng->ev_pending.emplace_back(ev0, ev1);
+    }
+    GSS_CUDA_TRY(cudaMemcpyAsync(eng->h_counts.ptr, eng->counts.ptr, sizeof(uint32_t) * eng->n_parts,
+                                 cudaMemcpyDeviceToHost, eng->stream));
+    eng->launches++;
+    eng->pass_pending = true;
+    return GSS_OK;
+}
+
+int gss_check_wait(gss_engine *eng, int64_t *n_reports) {
+    if (!eng) return set_error(GSS_ERR_INVALID, "engine is NULL");
+    GSS_TRY(ensure_device(eng));
+    GSS_CUDA_TRY(cudaStreamSynchronize(eng->stream));
+    eng->pass_pending = false;
+    const uint32_t *hc = (const uint32_t *) eng->h_counts.ptr;
+    int64_t total = 0;
+    bool overflow = false;
+    for (uint32_t p = 0; p < eng->n_parts; p++) {
+        total += hc[p];
+        if (hc[p] > eng->cap_per_part) overflow = true;
+    }
+    if (n_reports) *n_reports = total;
+    if (overflow) {
+        // Next automatic capacity: twice what this pass needed.
+        eng->requested_cap = std::max<int64_t>(eng->requested_cap, total * 2 + eng->n_parts * 1024);
+        return set_error(GSS_ERR_OVERFLOW, "report queues overflowed (%lld reports, %u per partition)",
+                         (long long) total, eng->cap_per_part);
+    }
+    return GSS_OK;
+}
+
+int gss_check_copy_reports(gss_engine *eng, gss_report *out, int64_t cap, int64_t *n_reports) {
+    if (!eng || (cap > 0 && !out)) return set_error(GSS_ERR_INVALID, "bad arguments to gss_check_copy_reports");
+    int64_t total = 0;
+    GSS_TRY(gss_check_wait(eng, &total));
+    if (n_reports) *n_reports = total;
+    if (total > cap) return set_error(GSS_ERR_OVERFLOW, "output holds %lld records, pass has %lld", (long long) cap,
+                                      (long long) total);
+    const uint32_t *hc = (const uint32_t *) eng->h_counts.ptr;
+    int64_t pos = 0;
+    for (uint32_t p = 0; p < eng->n_parts; p++) {
+        if (hc[p] == 0) continue;
+        GSS_CUDA_TRY(cudaMemcpyAsync(out + pos, (gss_report *) eng->reports.ptr + (size_t) p * eng->cap_per_part,
+                                     (size_t) hc[p] * sizeof(gss_report), cudaMemcpyDeviceToHost, eng->stream));
+        pos += hc[p];
+    }
+    GSS_CUDA_TRY(cudaStreamSynchronize(eng->stream));
+    return GSS_OK;
+}
+
+int gss_check_pass_host(gss_engine *eng, const uint32_t *state, int64_t n_vars, int n_words, const uint32_t *start,
+                        const int32_t *solver_of_word, gss_report *out, int64_t cap, int64_t *n_reports) {
+    GSS_TRY(gss_state_set(eng, state, n_vars, n_words, start, solver_of_word, 0));
+    for (int attempt = 0; attempt < 4; attempt++) {
+        GSS_TRY(gss_check_launch(eng));
+        int64_t total = 0;
+        int rc = gss_check_wait(eng, &total);
+        if (rc == GSS_ERR_OVERFLOW) continue;  // capacity was raised; run the pass again
+        GSS_TRY(rc);
+        return gss_check_copy_reports(eng, out, cap, n_reports);
+    }
+    return set_error(GSS_ERR_OVERFLOW, "report queues kept overflowing");
+}
+
+}  // extern "C"

@@ -1,0 +1,155 @@
+"""Parity of the CUDA check pass with the CPU oracle, through the C ABI.
+
+Bit-exact: the set of (clause, word, slot-mask) records must equal the
+oracle's. Covers the small plain-check workload in full, the at-scale
+workload at reduced size and edge cases (unit clauses, the longest clause,
+partial words, unstarted slots, empty inputs, queue overflow).
+"""
+import numpy as np
+import pytest
+
+import oracle
+from gpusharesat_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def _gpu_reports(engine, wl, capacity=0):
+    import gpusharesat_gb300 as g
+    engine.set_db(wl.lits, wl.offsets)
+    engine.set_state(wl.state, wl.start, wl.solver_of_word)
+    engine.set_capacity(capacity)
+    rep = engine.check()
+    return g.sort_reports(rep)
+
+
+def _assert_same(gpu, ref, wl=None):
+    assert len(gpu) == len(ref), (len(gpu), len(ref))
+    for f in ("clause", "word", "mask"):
+        np.testing.assert_array_equal(gpu[f], ref[f], err_msg=f)
+    if wl is not None and len(gpu):
+        np.testing.assert_array_equal(gpu["solver"], wl.solver_of_word[gpu["word"]])
+
+
+def test_small_workload_parity(engine):
+    wl = W.make_small(seed=0)
+    ref = oracle.check(wl.lits, wl.offsets, wl.state, wl.start, n_threads=8)
+    gpu = _gpu_reports(engine, wl)
+    _assert_same(gpu, ref, wl)
+    # planted clauses whose last literal is false or undefined must report
+    assert len(ref) > 0
+
+
+def test_scale_workload_reduced_parity(engine):
+    wl = W.make_scale(seed=1, n_vars=2 ** 16, n_clauses=200_000)
+    ref = oracle.check(wl.lits, wl.offsets, wl.state, wl.start, n_threads=8)
+    gpu = _gpu_reports(engine, wl)
+    _assert_same(gpu, ref, wl)
+
+
+@pytest.mark.parametrize("n_words", [1, 3, 33, 70])
+def test_word_counts(engine, n_words):
+    rng = np.random.default_rng(100 + n_words)
+    n_vars = 3000
+    lengths = W.lengths_small(rng, 5000)
+    lits, offsets = W.distinct_var_clauses(rng, lengths, n_vars)
+    state = W.random_state(rng, n_vars, n_words, rng.uniform(0.3, 0.95, 32 * n_words))
+    start = rng.integers(0, 2 ** 32, size=n_words, dtype=np.uint32)  # ragged started slots
+    start[0] = 0xFFFFFFFF
+    wl = W.Workload("words", n_vars, lits, offsets, state, start,
+                    (np.arange(n_words) // 2).astype(np.int32), (n_words + 1) // 2)
+    ref = oracle.check(lits, offsets, state, start)
+    gpu = _gpu_reports(engine, wl)
+    _assert_same(gpu, ref, wl)
+
+
+def test_unit_and_long_clauses(engine, lib):
+    rng = np.random.default_rng(7)
+    n_vars = 20000
+    maxlen = lib.gss_max_clause_len()
+    lengths = np.array([1] * 500 + [2] * 500 + [maxlen, maxlen - 1, 100, 101, 255, 256, 257], dtype=np.int64)
+    lits, offsets = W.distinct_var_clauses(rng, lengths, n_vars)
+    # mostly-false assignments so that long clauses survive a while
+    state = W.random_state(rng, n_vars, 4, np.full(128, 0.999))
+    # make every long clause all-false under slot 5 of word 2
+    for c in range(1000, len(lengths)):
+        for i in range(offsets[c], offsets[c + 1]):
+            v = lits[i] >> 1
+            state[v, 2, 0] |= np.uint32(1 << 5)
+            t = (int(state[v, 2, 1]) >> 5) & 1
+            lits[i] = 2 * v + t
+    start = np.full(4, 0xFFFFFFFF, dtype=np.uint32)
+    wl = W.Workload("edge", n_vars, lits, offsets, state, start, np.arange(4, dtype=np.int32), 4)
+    ref = oracle.check(lits, offsets, state, start)
+    gpu = _gpu_reports(engine, wl)
+    _assert_same(gpu, ref, wl)
+    long_ids = set(range(1000, len(lengths)))
+    hit = {int(r["clause"]) for r in ref if r["word"] == 2 and (int(r["mask"]) >> 5) & 1}
+    assert long_ids <= hit
+
+
+def test_unstarted_slots_never_report(engine):
+    rng = np.random.default_rng(3)
+    n_vars = 500
+    lits, offsets = W.distinct_var_clauses(rng, np.ones(400, dtype=np.int64), n_vars)
+    state = np.zeros((n_vars, 2, 2), dtype=np.uint32)  # everything undefined: units report everywhere
+    start = np.array([0x0000F00F, 0], dtype=np.uint32)
+    wl = W.Workload("unstarted", n_vars, lits, offsets, state, start, np.zeros(2, np.int32), 1)
+    gpu = _gpu_reports(engine, wl)
+    assert len(gpu) == 400
+    assert set(gpu["mask"].tolist()) == {0x0000F00F}
+    assert set(gpu["word"].tolist()) == {0}
+
+
+def test_empty_inputs(engine):
+    wl = W.Workload("empty", 10, np.zeros(0, np.int32), np.zeros(1, np.int64),
+                    np.zeros((10, 1, 2), np.uint32), np.full(1, 0xFFFFFFFF, np.uint32), np.zeros(1, np.int32), 1)
+    assert len(_gpu_reports(engine, wl)) == 0
+    rng = np.random.default_rng(1)
+    lits, offsets = W.distinct_var_clauses(rng, np.full(10, 3), 10)
+    wl0 = W.Workload("nowords", 10, lits, offsets, np.zeros((10, 0, 2), np.uint32), np.zeros(0, np.uint32),
+                     np.zeros(0, np.int32), 0)
+    assert len(_gpu_reports(engine, wl0)) == 0
+
+
+def test_overflow_reruns_to_same_result(engine):
+    wl = W.make_small(seed=5, n_clauses=20000)
+    ref = oracle.check(wl.lits, wl.offsets, wl.state, wl.start)
+    gpu = _gpu_reports(engine, wl, capacity=64)  # far too small: the engine grows and reruns
+    _assert_same(gpu, ref, wl)
+
+
+def test_rejects_bad_database(engine):
+    import gpusharesat_gb300 as g
+    with pytest.raises(g.GssError):
+        engine.set_db(np.array([-2], np.int32), np.array([0, 1], np.int64))
+    with pytest.raises(g.GssError):
+        engine.set_db(np.zeros(0, np.int32), np.array([0, 0], np.int64))  # empty clause
+    # a database with variables beyond the state is refused at launch
+    engine.set_db(np.array([2 * 50], np.int32), np.array([0, 1], np.int64))
+    engine.set_state(np.zeros((10, 1, 2), np.uint32), np.full(1, 1, np.uint32))
+    with pytest.raises(g.GssError):
+        engine.launch()
+
+
+def test_pass_through_host_buffers(engine):
+    wl = W.make_small(seed=9, n_clauses=30000)
+    import gpusharesat_gb300 as g
+    engine.set_db(wl.lits, wl.offsets)
+    engine.set_capacity(0)
+    rep = g.sort_reports(engine.pass_host(wl.state, wl.start, wl.solver_of_word))
+    ref = oracle.check(wl.lits, wl.offsets, wl.state, wl.start)
+    _assert_same(rep, ref, wl)
+
+
+import kat  # noqa: E402
+
+
+@pytest.mark.parametrize("case", kat.load_cases(), ids=lambda c: c["name"])
+def test_reference_known_answers_on_gpu(engine, case):
+    """The reference's own known-answer cases, through the C ABI on the GPU."""
+    lits, offsets, state, start, sow = kat.case_inputs(case)
+    wl = W.Workload(case["name"], case["n_vars"], lits, offsets, state, start, sow, int(sow.max()) + 1)
+    gpu = _gpu_reports(engine, wl)
+    got = oracle.expand(gpu)
+    np.testing.assert_array_equal(got, kat.expected_triples(case))
