@@ -52,6 +52,10 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=5)
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--kind", type=int, default=None, help="check kernel kind (0 direct, 1 tiled)")
+    p.add_argument("--lpc", type=int, default=0, help="lanes per clause (0 = automatic)")
+    p.add_argument("--depth", type=int, default=4, help="loads in flight (direct) or clause slots (tiled)")
+    p.add_argument("--flags", type=int, default=0, help="variant flags (1: L2 hint, 2: occupancy)")
     return p.parse_args()
 
 
@@ -233,6 +237,8 @@ def run_gpu(args):
     stream = torch.cuda.Stream()
     eng = g.Engine(local)
     eng.set_stream(stream.cuda_stream)
+    if args.kind is not None:
+        eng.set_variant(args.kind, args.lpc, args.depth, args.flags)
     eng.set_db(wl.lits, wl.offsets)
     eng.set_state(wl.state, wl.start, wl.solver_of_word)
     # size the queues: run once (grows on overflow)

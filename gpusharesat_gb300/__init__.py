@@ -21,6 +21,14 @@ GSS_ERR_OVERFLOW = -4
 GSS_ERR_STATE = -5
 GSS_ERR_NOT_FOUND = -6
 
+KERNEL_AUTO = -1
+KERNEL_DIRECT = 0
+KERNEL_TILED = 1
+KERNEL_WIDE4 = 2
+KERNEL_WIDE2 = 3
+VARIANT_L2_HINT = 1
+VARIANT_OCCUPANCY = 2
+
 REPORT_DTYPE = np.dtype([("clause", "<u4"), ("word", "<u4"), ("mask", "<u4"), ("solver", "<u4")])
 
 _lib = None
@@ -61,6 +69,7 @@ def load():
     _sig(lib, "gss_engine_launch_count", c_i64, vp)
     _sig(lib, "gss_engine_set_timing", c_int, vp, c_int)
     _sig(lib, "gss_engine_kernel_time", c_int, vp, vp, vp)
+    _sig(lib, "gss_engine_set_variant", c_int, vp, c_int, c_int, c_int, c_int)
     _sig(lib, "gss_db_set", c_int, vp, vp, vp, c_i64)
     _sig(lib, "gss_db_clause_count", c_i64, vp)
     _sig(lib, "gss_db_literal_count", c_i64, vp)
@@ -126,6 +135,10 @@ class Engine:
         n = ctypes.c_int64()
         _check(self.lib.gss_engine_kernel_time(self.h, ctypes.byref(ms), ctypes.byref(n)))
         return float(ms.value), int(n.value)
+
+    def set_variant(self, kind=-1, lanes_per_clause=0, depth=2, flags=0):
+        """kind: KERNEL_*; lanes_per_clause 0 = automatic; flags: VARIANT_* bits."""
+        _check(self.lib.gss_engine_set_variant(self.h, kind, lanes_per_clause, depth, int(flags)))
 
     def set_db(self, lits, offsets):
         lits = np.ascontiguousarray(lits, dtype=np.int32)

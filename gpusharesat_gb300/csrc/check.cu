@@ -1,4 +1,4 @@
-// The clause-check kernel: every clause of the database against every started
+// The clause-check kernels: every clause of the database against every started
 // assignment slot, reporting the slots where all literals are false or where
 // exactly one is undefined and the rest are false.
 //
@@ -9,24 +9,39 @@
 //     report    = allFalse | oneUndef
 // with the literal's value from the variable's {isDef, isTrue} word as in
 // GpuRunner.cu:74-81. The scan of a clause stops once no slot can report
-// (GpuRunner.cu:82-84). The reference walks one clause per thread and first
-// tests a 32-bit cross-solver aggregate (GpuRunner.cu:152-170); here one warp
-// walks one clause and each lane owns one 32-slot word, so the 32 lanes read a
-// variable's state as one contiguous 256-byte row, and no prefilter is needed.
+// (GpuRunner.cu:82-84).
+//
+// Mapping. The reference walks one clause per thread and first tests a 32-bit
+// cross-solver aggregate (GpuRunner.cu:152-170), then each solver's words
+// one by one. Here a group of LPC lanes walks one clause and each lane owns one
+// 32-slot word of a "slot block" of LPC words; a warp holds 32/LPC clauses of
+// equal or similar length (the database is sorted by length, like the
+// reference's per-size buckets, Clauses.cu:47-126). The state of one slot block
+// is stored block-major, [block][var][LPC words]{isDef,isTrue}, so a group reads
+// a variable's LPC words as one contiguous run of 8*LPC bytes, and the blocks
+// are scanned one after another so that the block being scanned can stay
+// resident in L2 while the clause literals stream past it (evict-first hint).
+// No prefilter is needed: a lane that has no slot left stops loading, and a
+// group stops reading literals once all its lanes are done.
+//
+// Memory-level parallelism: a group issues the state loads of G literals
+// before it consumes any of them (lanes that die inside the G are harmless: the
+// loaded words are simply not used), so a warp has up to G independent
+// gathers in flight instead of one.
 //
 // Reports: each warp stages its records in shared memory and reserves room in
-// global memory with one atomicAdd per flush on its block's partition
-// counter (the reference does one atomicAdd per report, Reporter.cuh:41-49,
-// and drops reports when a category is full; here nothing is dropped: a full
-// partition keeps counting so the host sees the overflow and runs again).
+// global memory with one atomicAdd per flush on its block's partition counter.
+// The reference does one atomicAdd per report and drops reports when a
+// category is full (Reporter.cuh:41-49); here nothing is dropped: a full
+// partition keeps counting, so the host sees the overflow and runs again.
 #include "common.h"
 
 namespace gss {
 
 namespace {
 
-constexpr int kWarps = 8;          // warps per block
-constexpr int kStage = 128;        // staged records per warp
+constexpr int kWarps = 8;     // warps per block
+constexpr int kStage = 128;   // staged records per warp
 constexpr unsigned kFull = 0xFFFFFFFFu;
 
 __device__ __forceinline__ unsigned lanemask_lt() {
@@ -35,8 +50,45 @@ __device__ __forceinline__ unsigned lanemask_lt() {
     return m;
 }
 
-__device__ __forceinline__ void flush_stage(gss_report *stage, uint32_t n, gss_report *out,
-                                            uint32_t *counter, uint32_t cap, int lane) {
+// L2 eviction-priority policies (createpolicy): the slot block's state is
+// kept (evict-last), the clause literals stream past it (evict-first).
+__device__ __forceinline__ uint64_t policy_evict_last() {
+    uint64_t p;
+    asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+
+__device__ __forceinline__ uint64_t policy_evict_first() {
+    uint64_t p;
+    asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+
+// State gather: read-only, no L1 allocation (random rows are not reused
+// within an SM), with the L2 policy when hints are on.
+__device__ __forceinline__ uint2 ld_state(const uint2 *p, bool hint, uint64_t pol) {
+    uint2 v;
+    if (hint) {
+        asm("ld.global.nc.L1::no_allocate.L2::cache_hint.v2.u32 {%0, %1}, [%2], %3;"
+            : "=r"(v.x), "=r"(v.y) : "l"(p), "l"(pol));
+    } else {
+        asm("ld.global.nc.v2.u32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "l"(p));
+    }
+    return v;
+}
+
+__device__ __forceinline__ int32_t ld_lit(const int32_t *p, bool hint, uint64_t pol) {
+    int32_t v;
+    if (hint) {
+        asm("ld.global.nc.L1::no_allocate.L2::cache_hint.s32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
+    } else {
+        asm("ld.global.nc.s32 %0, [%1];" : "=r"(v) : "l"(p));
+    }
+    return v;
+}
+
+__device__ __forceinline__ void flush_stage(gss_report *stage, uint32_t n, gss_report *out, uint32_t *counter,
+                                            uint32_t cap, int lane) {
     __syncwarp();
     uint32_t base = 0;
     if (lane == 0) base = atomicAdd(counter, n);
@@ -48,47 +100,78 @@ __device__ __forceinline__ void flush_stage(gss_report *stage, uint32_t n, gss_r
     __syncwarp();
 }
 
-__global__ void __launch_bounds__(kWarps * 32)
-check_csr_kernel(CheckArgs a, uint32_t n_wblocks) {
+template <int LPC, int G>
+__global__ void __launch_bounds__(kWarps * 32) check_kernel(CheckArgs a) {
+    static_assert(LPC == 2 || LPC == 4 || LPC == 8 || LPC == 16 || LPC == 32, "lanes per clause");
+    static_assert(G >= 1 && G <= LPC, "prefetch depth");
+    constexpr int CPW = 32 / LPC;  // clauses per warp
     __shared__ gss_report stage_all[kWarps][kStage];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
+    const int sub = lane % LPC;     // word within the slot block
+    const int grp = lane / LPC;     // clause within the warp
+    const int gbase = grp * LPC;    // first lane of this clause group
     gss_report *stage = stage_all[wib];
     const uint32_t part = blockIdx.x % a.n_parts;
     gss_report *out = a.out + (size_t) part * a.cap_per_part;
     uint32_t *counter = a.counts + part;
     uint32_t nstaged = 0;
+    const bool hint = a.cache_hints != 0;
+    const uint64_t pol_keep = policy_evict_last();
+    const uint64_t pol_stream = policy_evict_first();
 
-    const uint64_t n_tasks = (uint64_t) a.n_clauses * n_wblocks;
+    const uint32_t n_groups = (a.n_clauses + CPW - 1) / CPW;
+    const uint64_t n_tasks = (uint64_t) n_groups * a.n_blocks;
     const uint64_t stride = (uint64_t) gridDim.x * kWarps;
     for (uint64_t task = (uint64_t) blockIdx.x * kWarps + wib; task < n_tasks; task += stride) {
-        const uint32_t c = (uint32_t) (task / n_wblocks);
-        const uint32_t wb = (uint32_t) (task - (uint64_t) c * n_wblocks);
-        const uint32_t w = wb * 32 + lane;
-        const bool active = w < a.n_words;
-        uint32_t all_false = active ? __ldg(a.start + w) : 0u;
+        // Slot block outermost: all warps sweep block 0 first, then block 1...
+        const uint32_t blk = (uint32_t) (task / n_groups);
+        const uint32_t g = (uint32_t) (task - (uint64_t) blk * n_groups);
+        const uint32_t c = g * CPW + grp;
+        const bool valid = c < a.n_clauses;
+        const uint32_t w = blk * LPC + sub;
+        uint32_t all_false = valid ? __ldg(a.start + w) : 0u;  // start is padded to n_blocks*LPC
         uint32_t one_undef = 0;
-        const int64_t b = __ldg(a.offsets + c);
-        const int64_t e = __ldg(a.offsets + c + 1);
-        for (int64_t base = b; base < e; base += 32) {
-            const int32_t mine = (base + lane < e) ? __ldg(a.lits + base + lane) : 0;
-            const int n = (int) min((int64_t) 32, e - base);
-            bool alive = true;
-            for (int k = 0; k < n; k++) {
-                const uint32_t lit = (uint32_t) __shfl_sync(kFull, mine, k);
-                if (all_false | one_undef) {
-                    const uint2 st = __ldg(a.state + (size_t) (lit >> 1) * a.n_words + w);
-                    const uint32_t f = ((lit & 1u) ? st.y : ~st.y) & st.x;
-                    const uint32_t u = ~st.x;
-                    one_undef = (all_false & u) | (one_undef & f);
-                    all_false &= f;
+        int64_t pos = 0, end = 0;
+        if (valid) {
+            pos = __ldg(a.offsets + c);
+            end = __ldg(a.offsets + c + 1);
+        }
+        const uint2 *rows = a.state + (size_t) blk * a.n_vars * LPC + sub;
+        while (true) {
+            const bool mine = (all_false | one_undef) != 0u && pos < end;
+            const unsigned live = __ballot_sync(kFull, mine);
+            if (live == 0u) break;
+            // LPC literals of this clause, one per lane of the group.
+            const int32_t chunk = (pos + sub < end) ? ld_lit(a.lits + pos + sub, hint, pol_stream) : 0;
+            const int navail = (int) min((int64_t) LPC, end - pos);
+#pragma unroll 1
+            for (int k0 = 0; k0 < LPC; k0 += G) {
+                // Groups that are done idle (no loads) until the whole warp is done.
+                if (!__any_sync(kFull, (all_false | one_undef) != 0u && k0 < navail)) break;
+                uint32_t lit[G];
+                uint2 st[G];
+#pragma unroll
+                for (int j = 0; j < G; j++) {
+                    lit[j] = (uint32_t) __shfl_sync(kFull, chunk, gbase + k0 + j);
                 }
-                if (!__any_sync(kFull, all_false | one_undef)) {
-                    alive = false;
-                    break;
+                const bool alive = (all_false | one_undef) != 0u;
+#pragma unroll
+                for (int j = 0; j < G; j++) {
+                    st[j] = make_uint2(0u, 0u);
+                    if (alive && k0 + j < navail) st[j] = ld_state(rows + (size_t) (lit[j] >> 1) * LPC, hint, pol_keep);
+                }
+#pragma unroll
+                for (int j = 0; j < G; j++) {
+                    if (k0 + j < navail) {
+                        const uint32_t f = ((lit[j] & 1u) ? st[j].y : ~st[j].y) & st[j].x;
+                        const uint32_t u = ~st[j].x;
+                        one_undef = (all_false & u) | (one_undef & f);
+                        all_false &= f;
+                    }
                 }
             }
-            if (!alive) break;
+            pos += LPC;
         }
         const uint32_t rep = all_false | one_undef;
         const unsigned bal = __ballot_sync(kFull, rep != 0u);
@@ -99,7 +182,7 @@ check_csr_kernel(CheckArgs a, uint32_t n_wblocks) {
             }
             if (rep) {
                 gss_report r;
-                r.clause = c;
+                r.clause = __ldg(a.orig + c);
                 r.word = w;
                 r.mask = rep;
                 r.solver = (uint32_t) __ldg(a.solver_of_word + w);
@@ -111,19 +194,259 @@ check_csr_kernel(CheckArgs a, uint32_t n_wblocks) {
     if (nstaged) flush_stage(stage, nstaged, out, counter, a.cap_per_part, lane);
 }
 
-}  // namespace
 
-int launch_check(const CheckArgs &a, cudaStream_t stream, int sm_count) {
-    if (a.n_clauses == 0 || a.n_words == 0) return GSS_OK;
-    const uint32_t n_wblocks = (a.n_words + 31) / 32;
+// Wide variant: each lane owns WPL consecutive 32-slot words (WPL = 4: one
+// 256-bit load of {isDef, isTrue} x 4 per literal), a group of LPC lanes owns
+// a clause, and the slot block is LPC * WPL words. With WPL = 4 and LPC = 8 a
+// warp checks 4 clauses against all 1024 slots of a 32-word pass with one
+// load instruction per literal step: 4 rows of 256 contiguous bytes.
+template <int WPL>
+struct Row;
+template <>
+struct Row<1> {
+    uint32_t v[2];
+};
+template <>
+struct Row<2> {
+    uint32_t v[4];
+};
+template <>
+struct Row<4> {
+    uint32_t v[8];
+};
+
+template <int WPL>
+__device__ __forceinline__ void ld_row(const uint2 *p, Row<WPL> &r);
+template <>
+__device__ __forceinline__ void ld_row<1>(const uint2 *p, Row<1> &r) {
+    asm("ld.global.nc.L1::no_allocate.v2.u32 {%0, %1}, [%2];" : "=r"(r.v[0]), "=r"(r.v[1]) : "l"(p));
+}
+template <>
+__device__ __forceinline__ void ld_row<2>(const uint2 *p, Row<2> &r) {
+    asm("ld.global.nc.L1::no_allocate.v4.u32 {%0, %1, %2, %3}, [%4];"
+        : "=r"(r.v[0]), "=r"(r.v[1]), "=r"(r.v[2]), "=r"(r.v[3]) : "l"(p));
+}
+template <>
+__device__ __forceinline__ void ld_row<4>(const uint2 *p, Row<4> &r) {
+    asm("ld.global.nc.L1::no_allocate.v8.u32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=r"(r.v[0]), "=r"(r.v[1]), "=r"(r.v[2]), "=r"(r.v[3]), "=r"(r.v[4]), "=r"(r.v[5]), "=r"(r.v[6]),
+          "=r"(r.v[7])
+        : "l"(p));
+}
+
+template <int WPL, int LPC, int G, int MINB>
+__global__ void __launch_bounds__(kWarps * 32, MINB) check_wide_kernel(CheckArgs a) {
+    constexpr int CPW = 32 / LPC;
+    constexpr int BW = WPL * LPC;
+    static_assert(G >= 1 && G <= LPC, "depth");
+    __shared__ gss_report stage_all[kWarps][kStage];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int sub = lane % LPC;
+    const int grp = lane / LPC;
+    const int gbase = grp * LPC;
+    gss_report *stage = stage_all[wib];
+    const uint32_t part = blockIdx.x % a.n_parts;
+    gss_report *out = a.out + (size_t) part * a.cap_per_part;
+    uint32_t *counter = a.counts + part;
+    uint32_t nstaged = 0;
+
+    const uint32_t n_groups = (a.n_clauses + CPW - 1) / CPW;
+    const uint64_t n_tasks = (uint64_t) n_groups * a.n_blocks;
+    const uint64_t stride = (uint64_t) gridDim.x * kWarps;
+    for (uint64_t task = (uint64_t) blockIdx.x * kWarps + wib; task < n_tasks; task += stride) {
+        const uint32_t blk = (uint32_t) (task / n_groups);
+        const uint32_t g = (uint32_t) (task - (uint64_t) blk * n_groups);
+        const uint32_t c = g * CPW + grp;
+        const bool valid = c < a.n_clauses;
+        const uint32_t w0 = blk * BW + sub * WPL;
+        uint32_t af[WPL], ou[WPL];
+#pragma unroll
+        for (int j = 0; j < WPL; j++) {
+            af[j] = valid ? __ldg(a.start + w0 + j) : 0u;
+            ou[j] = 0u;
+        }
+        uint32_t pos = 0, end = 0;
+        if (valid) {
+            pos = (uint32_t) __ldg(a.offsets + c);
+            end = (uint32_t) __ldg(a.offsets + c + 1);
+        }
+        const uint2 *rows = a.state + (size_t) blk * a.n_vars * BW + sub * WPL;
+        while (true) {
+            bool alive = false;
+#pragma unroll
+            for (int j = 0; j < WPL; j++) alive |= (af[j] | ou[j]) != 0u;
+            if (!__any_sync(kFull, alive && pos < end)) break;
+            const int32_t chunk = (pos + sub < end) ? __ldg(a.lits + pos + sub) : 0;
+            const int navail = (int) min((uint32_t) LPC, end > pos ? end - pos : 0u);
+#pragma unroll 1
+            for (int k0 = 0; k0 < LPC; k0 += G) {
+                alive = false;
+#pragma unroll
+                for (int j = 0; j < WPL; j++) alive |= (af[j] | ou[j]) != 0u;
+                if (!__any_sync(kFull, alive && k0 < navail)) break;
+                uint32_t lit[G];
+                Row<WPL> st[G];
+#pragma unroll
+                for (int i = 0; i < G; i++) lit[i] = (uint32_t) __shfl_sync(kFull, chunk, gbase + k0 + i);
+#pragma unroll
+                for (int i = 0; i < G; i++) {
+#pragma unroll
+                    for (int q = 0; q < 2 * WPL; q++) st[i].v[q] = 0u;
+                    if (alive && k0 + i < navail) ld_row<WPL>(rows + (size_t) (lit[i] >> 1) * BW, st[i]);
+                }
+#pragma unroll
+                for (int i = 0; i < G; i++) {
+                    if (k0 + i < navail) {
+                        const bool neg = (lit[i] & 1u) != 0u;
+#pragma unroll
+                        for (int j = 0; j < WPL; j++) {
+                            const uint32_t d = st[i].v[2 * j], t = st[i].v[2 * j + 1];
+                            const uint32_t f = (neg ? t : ~t) & d;
+                            ou[j] = (af[j] & ~d) | (ou[j] & f);
+                            af[j] &= f;
+                        }
+                    }
+                }
+            }
+            pos += LPC;
+        }
+#pragma unroll
+        for (int j = 0; j < WPL; j++) {
+            const uint32_t rep = af[j] | ou[j];
+            const unsigned bal = __ballot_sync(kFull, rep != 0u);
+            if (bal) {
+                if (nstaged + 32 > (uint32_t) kStage) {
+                    flush_stage(stage, nstaged, out, counter, a.cap_per_part, lane);
+                    nstaged = 0;
+                }
+                if (rep) {
+                    gss_report r;
+                    r.clause = __ldg(a.orig + c);
+                    r.word = w0 + j;
+                    r.mask = rep;
+                    r.solver = (uint32_t) __ldg(a.solver_of_word + w0 + j);
+                    stage[nstaged + __popc(bal & lanemask_lt())] = r;
+                }
+                nstaged += __popc(bal);
+            }
+        }
+    }
+    if (nstaged) flush_stage(stage, nstaged, out, counter, a.cap_per_part, lane);
+}
+
+template <int WPL, int LPC, int G, int MINB>
+int launch_wide_variant(const CheckArgs &a, cudaStream_t stream, int sm_count) {
     int per_sm = 0;
-    GSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, check_csr_kernel, kWarps * 32, 0));
+    GSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, check_wide_kernel<WPL, LPC, G, MINB>,
+                                                               kWarps * 32, 0));
     if (per_sm < 1) per_sm = 1;
-    const uint64_t n_tasks = (uint64_t) a.n_clauses * n_wblocks;
+    constexpr int CPW = 32 / LPC;
+    const uint64_t n_tasks = (uint64_t) ((a.n_clauses + CPW - 1) / CPW) * a.n_blocks;
     uint64_t blocks = (uint64_t) sm_count * per_sm;
     const uint64_t need = (n_tasks + kWarps - 1) / kWarps;
     if (blocks > need) blocks = need;
-    check_csr_kernel<<<(unsigned) blocks, kWarps * 32, 0, stream>>>(a, n_wblocks);
+    if (blocks < 1) blocks = 1;
+    check_wide_kernel<WPL, LPC, G, MINB><<<(unsigned) blocks, kWarps * 32, 0, stream>>>(a);
+    GSS_CUDA_TRY(cudaGetLastError());
+    return GSS_OK;
+}
+
+// Host layout [n_vars][n_words]{isDef,isTrue} -> block-major
+// [n_blocks][n_vars][lpc]{isDef,isTrue}, words past n_words zero.
+__global__ void relayout_kernel(const uint2 *__restrict__ src, uint2 *__restrict__ dst, uint32_t n_vars,
+                                uint32_t n_words, uint32_t lpc, uint32_t n_blocks) {
+    const uint64_t total = (uint64_t) n_blocks * n_vars * lpc;
+    for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (uint64_t) gridDim.x * blockDim.x) {
+        const uint32_t s = (uint32_t) (i % lpc);
+        const uint64_t r = i / lpc;
+        const uint32_t v = (uint32_t) (r % n_vars);
+        const uint32_t b = (uint32_t) (r / n_vars);
+        const uint32_t w = b * lpc + s;
+        dst[i] = (w < n_words) ? src[(uint64_t) v * n_words + w] : make_uint2(0u, 0u);
+    }
+}
+
+template <int LPC, int G>
+int launch_variant(const CheckArgs &a, cudaStream_t stream, int sm_count) {
+    int per_sm = 0;
+    GSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, check_kernel<LPC, G>, kWarps * 32, 0));
+    if (per_sm < 1) per_sm = 1;
+    constexpr int CPW = 32 / LPC;
+    const uint64_t n_tasks = (uint64_t) ((a.n_clauses + CPW - 1) / CPW) * a.n_blocks;
+    uint64_t blocks = (uint64_t) sm_count * per_sm;
+    const uint64_t need = (n_tasks + kWarps - 1) / kWarps;
+    if (blocks > need) blocks = need;
+    if (blocks < 1) blocks = 1;
+    check_kernel<LPC, G><<<(unsigned) blocks, kWarps * 32, 0, stream>>>(a);
+    GSS_CUDA_TRY(cudaGetLastError());
+    return GSS_OK;
+}
+
+}  // namespace
+
+// Wide variants: (words per lane, lanes per clause, depth, occupancy hint).
+bool valid_wide_variant(int wpl, int lpc, int g, int occ) {
+    if (occ != 0 && occ != 1) return false;
+    if (wpl == 4 && lpc == 8) return g == 1 || g == 2 || g == 4;
+    if (wpl == 4 && lpc == 4) return g == 1 || g == 2 || g == 4;
+    if (wpl == 4 && lpc == 2) return g == 1 || g == 2;
+    if (wpl == 2 && lpc == 16) return g == 1 || g == 2 || g == 4;
+    if (wpl == 2 && lpc == 8) return g == 1 || g == 2 || g == 4;
+    if (wpl == 1 && lpc == 32) return g == 1 || g == 2 || g == 4;
+    return false;
+}
+
+int launch_check_wide(const CheckArgs &a, int wpl, int occ, cudaStream_t stream, int sm_count) {
+    if (a.n_clauses == 0 || a.n_blocks == 0) return GSS_OK;
+#define GSS_WV(W, L, GG)                                                                      \
+    if (wpl == W && a.lpc == L && a.g == GG)                                                  \
+        return occ ? launch_wide_variant<W, L, GG, 8>(a, stream, sm_count)                    \
+                   : launch_wide_variant<W, L, GG, 1>(a, stream, sm_count);
+    GSS_WV(4, 8, 1) GSS_WV(4, 8, 2) GSS_WV(4, 8, 4)
+    GSS_WV(4, 4, 1) GSS_WV(4, 4, 2) GSS_WV(4, 4, 4)
+    GSS_WV(4, 2, 1) GSS_WV(4, 2, 2)
+    GSS_WV(2, 16, 1) GSS_WV(2, 16, 2) GSS_WV(2, 16, 4)
+    GSS_WV(2, 8, 1) GSS_WV(2, 8, 2) GSS_WV(2, 8, 4)
+    GSS_WV(1, 32, 1) GSS_WV(1, 32, 2) GSS_WV(1, 32, 4)
+#undef GSS_WV
+    return set_error(GSS_ERR_INVALID, "no wide kernel variant for %d words per lane, %d lanes, depth %d", wpl,
+                     a.lpc, a.g);
+}
+
+bool valid_variant(int lpc, int g) {
+    switch (lpc) {
+        case 2: return g == 1 || g == 2;
+        case 4: return g == 1 || g == 2 || g == 4;
+        case 8: return g == 1 || g == 2 || g == 4 || g == 8;
+        case 16: return g == 1 || g == 2 || g == 4 || g == 8;
+        case 32: return g == 1 || g == 2 || g == 4 || g == 8;
+        default: return false;
+    }
+}
+
+int launch_check(const CheckArgs &a, cudaStream_t stream, int sm_count) {
+    if (a.n_clauses == 0 || a.n_blocks == 0) return GSS_OK;
+#define GSS_VARIANT(L, GG) \
+    if (a.lpc == L && a.g == GG) return launch_variant<L, GG>(a, stream, sm_count);
+    GSS_VARIANT(2, 1) GSS_VARIANT(2, 2)
+    GSS_VARIANT(4, 1) GSS_VARIANT(4, 2) GSS_VARIANT(4, 4)
+    GSS_VARIANT(8, 1) GSS_VARIANT(8, 2) GSS_VARIANT(8, 4) GSS_VARIANT(8, 8)
+    GSS_VARIANT(16, 1) GSS_VARIANT(16, 2) GSS_VARIANT(16, 4) GSS_VARIANT(16, 8)
+    GSS_VARIANT(32, 1) GSS_VARIANT(32, 2) GSS_VARIANT(32, 4) GSS_VARIANT(32, 8)
+#undef GSS_VARIANT
+    return set_error(GSS_ERR_INVALID, "no kernel variant for %d lanes per clause, depth %d", a.lpc, a.g);
+}
+
+int launch_relayout(const uint2 *src, uint2 *dst, uint32_t n_vars, uint32_t n_words, uint32_t lpc,
+                    uint32_t n_blocks, cudaStream_t stream, int sm_count) {
+    const uint64_t total = (uint64_t) n_blocks * n_vars * lpc;
+    if (total == 0) return GSS_OK;
+    uint64_t blocks = (total + 255) / 256;
+    const uint64_t cap = (uint64_t) sm_count * 8;
+    if (blocks > cap) blocks = cap;
+    relayout_kernel<<<(unsigned) blocks, 256, 0, stream>>>(src, dst, n_vars, n_words, lpc, n_blocks);
     GSS_CUDA_TRY(cudaGetLastError());
     return GSS_OK;
 }

@@ -14,6 +14,13 @@ namespace gss {
 // by default, the engine itself takes clauses up to this length.
 constexpr int kMaxClauseLen = 4096;
 
+// Tiles of the tiled check kernel: consecutive length-sorted clauses with at
+// most kTileLits literals (a longer clause gets a tile of its own and is read
+// from global memory). kBufLits leaves room for rounding a tile's literal
+// range out to 16-byte boundaries for the bulk copy.
+constexpr int kTileLits = 512;
+constexpr int kBufLits = kTileLits + 8;
+
 // Sets the calling thread's error message and returns `code`.
 int set_error(int code, const char *fmt, ...);
 
@@ -53,23 +60,42 @@ struct PinnedBuf {
     ~PinnedBuf() { release(); }
 };
 
-// Arguments of one check pass over a CSR clause database.
+// Arguments of one check pass over the length-sorted CSR clause database.
 struct CheckArgs {
-    const int32_t *lits;        // device, CSR literals
+    const int32_t *lits;        // device, CSR literals, clauses sorted by length
     const int64_t *offsets;     // device, n_clauses + 1
+    const uint32_t *orig;       // device, original index of each sorted clause
     uint32_t n_clauses;
-    const uint2 *state;         // device, [n_vars][n_words] {isDef, isTrue}
-    uint32_t n_words;
-    const uint32_t *start;      // device, [n_words]
-    const int32_t *solver_of_word;  // device, [n_words]
+    const uint2 *state;         // device, [n_blocks][n_vars][lpc] {isDef, isTrue}
+    uint32_t n_vars;
+    uint32_t n_blocks;          // slot blocks of lpc words
+    const uint32_t *start;      // device, [n_blocks * lpc], zero past the last word
+    const int32_t *solver_of_word;  // device, [n_blocks * lpc]
     gss_report *out;            // device, n_parts * cap_per_part records
     uint32_t *counts;           // device, n_parts counters (zeroed by the caller)
     uint32_t n_parts;
     uint32_t cap_per_part;
+    int lpc;                    // lanes (32-slot words) per clause
+    int g;                      // state loads in flight per lane (direct) / clause slots (tiled)
+    int cache_hints;            // L1/L2 eviction hints on the loads
+    // tiled kernel only
+    const uint32_t *tile_clause;  // device, n_tiles + 1: first sorted clause of each tile
+    const uint32_t *tile_lit;     // device, n_tiles + 1: first literal of each tile
+    uint32_t n_tiles;
+    uint32_t *err;                // device flag, set to nonzero when a bounded wait gives up
 };
 
 // Launches the check kernel on `stream` (the counters must already be zero).
 // Returns a GSS status.
 int launch_check(const CheckArgs &a, cudaStream_t stream, int sm_count);
+bool valid_variant(int lpc, int g);
+int launch_check_tiled(const CheckArgs &a, cudaStream_t stream, int sm_count);
+int launch_check_wide(const CheckArgs &a, int wpl, int occ, cudaStream_t stream, int sm_count);
+bool valid_wide_variant(int wpl, int lpc, int g, int occ);
+bool valid_tiled_variant(int lpc, int k);
+
+// [n_vars][n_words] -> [n_blocks][n_vars][lpc], zero-padded words.
+int launch_relayout(const uint2 *src, uint2 *dst, uint32_t n_vars, uint32_t n_words, uint32_t lpc,
+                    uint32_t n_blocks, cudaStream_t stream, int sm_count);
 
 }  // namespace gss

@@ -97,14 +97,30 @@ struct gss_engine {
     cudaStream_t stream = nullptr;
     int64_t launches = 0;
 
-    // clause database (CSR)
-    DevBuf lits, offsets;
+    // clause database: CSR, clauses sorted by length (stable), with the
+    // original index of each sorted clause
+    DevBuf lits, offsets, orig;
     int64_t n_clauses = 0, n_lits = 0, max_var = -1;
+    // tiles of the tiled kernel (first clause / first literal of each tile)
+    DevBuf tile_clause, tile_lit;
+    uint32_t n_tiles = 0;
 
-    // assignment state
-    DevBuf state, start, solver_of_word;
+    // kernel variant: kind (GSS_KERNEL_*), lanes (words) per clause (0 = pick
+    // from the word count), loads in flight / clause slots, cache hints
+    int kind = GSS_KERNEL_AUTO, lpc = 0, g = 2, flags = 0;
+    DevBuf err;
+
+    // assignment state, block-major [n_blocks][n_vars][state_bw words]
+    DevBuf state, state_raw, start, solver_of_word;
     int64_t n_vars = 0;
     int n_words = 0;
+    int n_blocks = 0;
+    // effective variant the state was laid out for (resolved from the
+    // requested one and the word count by gss_state_set)
+    int state_kind = GSS_KERNEL_DIRECT;
+    int state_lpc = 0;  // lanes per clause
+    int state_g = 2;
+    int state_bw = 0;   // words per slot block
 
     // report queues: n_parts partitions of cap_per_part records
     DevBuf reports, counts;
@@ -121,6 +137,8 @@ struct gss_engine {
 };
 
 namespace {
+
+int words_per_lane(int kind) { return kind == GSS_KERNEL_WIDE4 ? 4 : kind == GSS_KERNEL_WIDE2 ? 2 : 1; }
 
 int ensure_device(gss_engine *eng) {
     GSS_CUDA_TRY(cudaSetDevice(eng->device));
@@ -141,7 +159,7 @@ int ensure_queues(gss_engine *eng) {
         eng->cap_per_part = (uint32_t) per;
     }
     GSS_TRY(eng->counts.reserve(sizeof(uint32_t) * eng->n_parts));
-    GSS_TRY(eng->h_counts.reserve(sizeof(uint32_t) * eng->n_parts));
+    GSS_TRY(eng->h_counts.reserve(sizeof(uint32_t) * (eng->n_parts + 1)));
     return GSS_OK;
 }
 
@@ -230,26 +248,68 @@ int gss_db_set(gss_engine *eng, const int32_t *lits, const int64_t *offsets, int
     if (!eng || !offsets || n_clauses < 0) return set_error(GSS_ERR_INVALID, "bad arguments to gss_db_set");
     if (n_clauses > 0xFFFFFFF0LL) return set_error(GSS_ERR_INVALID, "too many clauses (%lld)", (long long) n_clauses);
     if (offsets[0] != 0) return set_error(GSS_ERR_INVALID, "offsets[0] must be 0");
-    int64_t max_var = -1;
+    // Counting sort by length, stable: equal-length clauses keep their order,
+    // as in the reference's per-size buckets (Clauses.cu:47-51).
+    std::vector<int64_t> count(kMaxClauseLen + 2, 0);
     for (int64_t c = 0; c < n_clauses; c++) {
         int64_t len = offsets[c + 1] - offsets[c];
         if (len < 1 || len > kMaxClauseLen)
             return set_error(GSS_ERR_INVALID, "clause %lld has length %lld (allowed 1..%d)", (long long) c,
                              (long long) len, kMaxClauseLen);
+        count[len + 1]++;
     }
     const int64_t n_lits = offsets[n_clauses];
     if (n_lits > 0 && !lits) return set_error(GSS_ERR_INVALID, "lits is NULL");
+    if (n_lits > 0x7FFFFF00LL) return set_error(GSS_ERR_INVALID, "too many literals (%lld)", (long long) n_lits);
+    int64_t max_var = -1;
     for (int64_t i = 0; i < n_lits; i++) {
         if (lits[i] < 0) return set_error(GSS_ERR_INVALID, "literal %lld is negative", (long long) i);
         int64_t v = lits[i] >> 1;
         if (v > max_var) max_var = v;
     }
+    for (int L = 1; L <= kMaxClauseLen + 1; L++) count[L] += count[L - 1];
+    std::vector<uint32_t> orig(n_clauses);
+    for (int64_t c = 0; c < n_clauses; c++) {
+        int64_t len = offsets[c + 1] - offsets[c];
+        orig[count[len]++] = (uint32_t) c;
+    }
+    std::vector<int64_t> soff(n_clauses + 1);
+    std::vector<int32_t> slits(n_lits);
+    soff[0] = 0;
+    for (int64_t i = 0; i < n_clauses; i++) {
+        const int64_t c = orig[i];
+        const int64_t len = offsets[c + 1] - offsets[c];
+        memcpy(&slits[soff[i]], lits + offsets[c], len * sizeof(int32_t));
+        soff[i + 1] = soff[i] + len;
+    }
+    // Tiles: greedy runs of sorted clauses with at most kTileLits literals; a
+    // longer clause is a tile on its own.
+    std::vector<uint32_t> tclause, tlit;
+    for (int64_t i = 0; i < n_clauses;) {
+        tclause.push_back((uint32_t) i);
+        tlit.push_back((uint32_t) soff[i]);
+        int64_t j = i + 1;
+        while (j < n_clauses && soff[j + 1] - soff[i] <= kTileLits) j++;
+        i = j;
+    }
+    tclause.push_back((uint32_t) n_clauses);
+    tlit.push_back((uint32_t) n_lits);
     GSS_TRY(ensure_device(eng));
     GSS_CUDA_TRY(cudaStreamSynchronize(eng->stream));
-    GSS_TRY(eng->lits.reserve(std::max<int64_t>(n_lits, 1) * sizeof(int32_t)));
+    // 8 literals of zero padding: tile copies round their end up to 16 bytes
+    GSS_TRY(eng->lits.reserve((n_lits + 8) * sizeof(int32_t)));
+    GSS_CUDA_TRY(cudaMemset(eng->lits.ptr, 0, (n_lits + 8) * sizeof(int32_t)));
+    GSS_TRY(eng->tile_clause.reserve(tclause.size() * sizeof(uint32_t)));
+    GSS_TRY(eng->tile_lit.reserve(tlit.size() * sizeof(uint32_t)));
+    GSS_CUDA_TRY(cudaMemcpy(eng->tile_clause.ptr, tclause.data(), tclause.size() * sizeof(uint32_t),
+                            cudaMemcpyHostToDevice));
+    GSS_CUDA_TRY(cudaMemcpy(eng->tile_lit.ptr, tlit.data(), tlit.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    eng->n_tiles = (uint32_t) (tclause.size() - 1);
     GSS_TRY(eng->offsets.reserve((n_clauses + 1) * sizeof(int64_t)));
-    if (n_lits) GSS_CUDA_TRY(cudaMemcpy(eng->lits.ptr, lits, n_lits * sizeof(int32_t), cudaMemcpyHostToDevice));
-    GSS_CUDA_TRY(cudaMemcpy(eng->offsets.ptr, offsets, (n_clauses + 1) * sizeof(int64_t), cudaMemcpyHostToDevice));
+    GSS_TRY(eng->orig.reserve(std::max<int64_t>(n_clauses, 1) * sizeof(uint32_t)));
+    if (n_lits) GSS_CUDA_TRY(cudaMemcpy(eng->lits.ptr, slits.data(), n_lits * sizeof(int32_t), cudaMemcpyHostToDevice));
+    GSS_CUDA_TRY(cudaMemcpy(eng->offsets.ptr, soff.data(), (n_clauses + 1) * sizeof(int64_t), cudaMemcpyHostToDevice));
+    if (n_clauses) GSS_CUDA_TRY(cudaMemcpy(eng->orig.ptr, orig.data(), n_clauses * sizeof(uint32_t), cudaMemcpyHostToDevice));
     eng->n_clauses = n_clauses;
     eng->n_lits = n_lits;
     eng->max_var = max_var;
@@ -265,29 +325,117 @@ int gss_state_set(gss_engine *eng, const uint32_t *state, int64_t n_vars, int n_
     if (!eng || n_vars < 0 || n_words < 0 || (n_vars > 0 && n_words > 0 && !state) || (n_words > 0 && !start))
         return set_error(GSS_ERR_INVALID, "bad arguments to gss_state_set");
     if (n_words > 4096) return set_error(GSS_ERR_INVALID, "at most 4096 words (131072 slots) per pass");
+    if (n_vars > 0x7FFFFFFF) return set_error(GSS_ERR_INVALID, "too many variables");
     GSS_TRY(ensure_device(eng));
-    const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
-    const size_t sbytes = (size_t) n_vars * n_words * 2 * sizeof(uint32_t);
-    if (eng->pass_pending) GSS_CUDA_TRY(cudaStreamSynchronize(eng->stream));
-    GSS_TRY(eng->state.reserve(std::max<size_t>(sbytes, 8)));
-    GSS_TRY(eng->start.reserve(std::max<size_t>(n_words * sizeof(uint32_t), 4)));
-    GSS_TRY(eng->solver_of_word.reserve(std::max<size_t>(n_words * sizeof(int32_t), 4)));
-    if (sbytes) GSS_CUDA_TRY(cudaMemcpyAsync(eng->state.ptr, state, sbytes, kind, eng->stream));
-    if (n_words) {
-        GSS_CUDA_TRY(cudaMemcpyAsync(eng->start.ptr, start, n_words * sizeof(uint32_t), kind, eng->stream));
-        if (solver_of_word) {
-            GSS_CUDA_TRY(cudaMemcpyAsync(eng->solver_of_word.ptr, solver_of_word, n_words * sizeof(int32_t), kind,
-                                         eng->stream));
+    int kind = eng->kind, lpc = eng->lpc, depth = eng->g;
+    if (kind == GSS_KERNEL_AUTO) {
+        // Measured on GB300 for the at-scale workload: four words per lane with
+        // 256-bit loads, two loads in flight, is fastest once a clause spans
+        // eight or more words; below that one word per lane.
+        depth = 2;
+        if (n_words >= 8) {
+            kind = GSS_KERNEL_WIDE4;
+            lpc = n_words >= 32 ? 8 : n_words >= 16 ? 4 : 2;
         } else {
-            std::vector<int32_t> ident(n_words);
-            for (int w = 0; w < n_words; w++) ident[w] = w;
-            GSS_CUDA_TRY(cudaMemcpyAsync(eng->solver_of_word.ptr, ident.data(), n_words * sizeof(int32_t),
-                                         cudaMemcpyHostToDevice, eng->stream));
-            GSS_CUDA_TRY(cudaStreamSynchronize(eng->stream));
+            kind = GSS_KERNEL_DIRECT;
+            lpc = 0;
         }
     }
+    const int wpl = words_per_lane(kind);
+    if (lpc == 0) {
+        // one word per lane up to a full warp (wide kinds: 32 words per block)
+        lpc = 1;
+        if (wpl == 1) {
+            while (lpc < n_words && lpc < 32) lpc *= 2;
+        } else {
+            lpc = 32 / wpl;
+        }
+    }
+    const int bw = lpc * wpl;
+    const int n_blocks = (n_words + bw - 1) / bw;
+    const int padded = n_blocks * bw;
+    const size_t sbytes = (size_t) n_vars * n_words * 2 * sizeof(uint32_t);
+    const size_t bbytes = (size_t) n_blocks * n_vars * bw * 2 * sizeof(uint32_t);
+    if (eng->pass_pending) GSS_CUDA_TRY(cudaStreamSynchronize(eng->stream));
+    GSS_TRY(eng->state.reserve(std::max<size_t>(bbytes, 8)));
+    GSS_TRY(eng->start.reserve(std::max<size_t>(padded * sizeof(uint32_t), 4)));
+    GSS_TRY(eng->solver_of_word.reserve(std::max<size_t>(padded * sizeof(int32_t), 4)));
+    // start and solver_of_word, padded with zero words
+    std::vector<uint32_t> st(padded, 0u);
+    std::vector<int32_t> sw(padded, 0);
+    if (n_words) {
+        if (on_device) {
+            GSS_CUDA_TRY(cudaMemcpy(st.data(), start, n_words * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+            if (solver_of_word)
+                GSS_CUDA_TRY(cudaMemcpy(sw.data(), solver_of_word, n_words * sizeof(int32_t), cudaMemcpyDeviceToHost));
+        } else {
+            memcpy(st.data(), start, n_words * sizeof(uint32_t));
+            if (solver_of_word) memcpy(sw.data(), solver_of_word, n_words * sizeof(int32_t));
+        }
+        if (!solver_of_word)
+            for (int w = 0; w < n_words; w++) sw[w] = w;
+    }
+    if (padded) {
+        GSS_CUDA_TRY(cudaMemcpyAsync(eng->start.ptr, st.data(), padded * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                                     eng->stream));
+        GSS_CUDA_TRY(cudaMemcpyAsync(eng->solver_of_word.ptr, sw.data(), padded * sizeof(int32_t),
+                                     cudaMemcpyHostToDevice, eng->stream));
+    }
+    if (sbytes) {
+        if (n_blocks == 1 && n_words == bw) {
+            // block-major and host layouts coincide
+            GSS_CUDA_TRY(cudaMemcpyAsync(eng->state.ptr, state, sbytes,
+                                         on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, eng->stream));
+        } else {
+            const uint2 *src = (const uint2 *) state;
+            if (!on_device) {
+                GSS_TRY(eng->state_raw.reserve(sbytes));
+                GSS_CUDA_TRY(cudaMemcpyAsync(eng->state_raw.ptr, state, sbytes, cudaMemcpyHostToDevice, eng->stream));
+                src = (const uint2 *) eng->state_raw.ptr;
+            }
+            GSS_TRY(launch_relayout(src, (uint2 *) eng->state.ptr, (uint32_t) n_vars, (uint32_t) n_words,
+                                    (uint32_t) bw, (uint32_t) n_blocks, eng->stream, eng->sm_count));
+        }
+    }
+    // the host vectors above are pageable: the async copies from them complete before return
+    GSS_CUDA_TRY(cudaStreamSynchronize(eng->stream));
     eng->n_vars = n_vars;
     eng->n_words = n_words;
+    eng->n_blocks = n_blocks;
+    eng->state_kind = kind;
+    eng->state_lpc = lpc;
+    eng->state_g = depth;
+    eng->state_bw = bw;
+    return GSS_OK;
+}
+
+int gss_engine_set_variant(gss_engine *eng, int kind, int lanes_per_clause, int depth, int flags) {
+    if (!eng) return set_error(GSS_ERR_INVALID, "engine is NULL");
+    if (kind == GSS_KERNEL_AUTO) {
+        // nothing to validate: resolved per word count
+    } else if (kind == GSS_KERNEL_WIDE4 || kind == GSS_KERNEL_WIDE2) {
+        const int wpl = words_per_lane(kind);
+        const int l = lanes_per_clause ? lanes_per_clause : 32 / wpl;
+        if (!valid_wide_variant(wpl, l, depth, (flags & GSS_VARIANT_OCCUPANCY) ? 1 : 0))
+            return set_error(GSS_ERR_INVALID, "no wide kernel variant for %d words per lane, %d lanes, depth %d", wpl,
+                             l, depth);
+    } else if (kind == GSS_KERNEL_DIRECT) {
+        if (!valid_variant(lanes_per_clause, depth))
+            return set_error(GSS_ERR_INVALID, "no direct kernel variant for %d lanes per clause, depth %d",
+                             lanes_per_clause, depth);
+    } else if (kind == GSS_KERNEL_TILED) {
+        if (lanes_per_clause != 0 && !valid_tiled_variant(lanes_per_clause, depth))
+            return set_error(GSS_ERR_INVALID, "no tiled kernel variant for %d lanes per clause, %d slots",
+                             lanes_per_clause, depth);
+        if (lanes_per_clause == 0 && !valid_tiled_variant(32, depth))
+            return set_error(GSS_ERR_INVALID, "no tiled kernel variant with %d slots", depth);
+    } else {
+        return set_error(GSS_ERR_INVALID, "unknown kernel kind %d", kind);
+    }
+    eng->kind = kind;
+    eng->lpc = lanes_per_clause;
+    eng->g = depth;
+    eng->flags = flags;
     return GSS_OK;
 }
 
@@ -302,14 +450,30 @@ int gss_check_launch(gss_engine *eng) {
     if (eng->n_clauses > 0 && eng->max_var >= eng->n_vars)
         return set_error(GSS_ERR_INVALID, "database uses variable %lld but the state has %lld variables",
                          (long long) eng->max_var, (long long) eng->n_vars);
+    if (eng->n_words > 0 && eng->kind != GSS_KERNEL_AUTO &&
+        (eng->state_kind != eng->kind || (eng->lpc != 0 && eng->state_lpc != eng->lpc) || eng->state_g != eng->g))
+        return set_error(GSS_ERR_STATE, "the state was laid out for another kernel variant; set it again after "
+                         "changing the variant");
+    if (eng->state_kind == GSS_KERNEL_DIRECT && !valid_variant(eng->state_lpc, eng->state_g) && eng->n_words > 0)
+        return set_error(GSS_ERR_STATE, "no direct kernel variant for %d lanes per clause", eng->state_lpc);
     GSS_TRY(ensure_device(eng));
     GSS_TRY(ensure_queues(eng));
     CheckArgs a;
     a.lits = (const int32_t *) eng->lits.ptr;
     a.offsets = (const int64_t *) eng->offsets.ptr;
+    a.orig = (const uint32_t *) eng->orig.ptr;
     a.n_clauses = (uint32_t) eng->n_clauses;
     a.state = (const uint2 *) eng->state.ptr;
-    a.n_words = (uint32_t) eng->n_words;
+    a.n_vars = (uint32_t) eng->n_vars;
+    a.n_blocks = (uint32_t) eng->n_blocks;
+    a.lpc = eng->state_lpc;
+    a.g = eng->state_g;
+    a.cache_hints = (eng->flags & GSS_VARIANT_L2_HINT) ? 1 : 0;
+    a.tile_clause = (const uint32_t *) eng->tile_clause.ptr;
+    a.tile_lit = (const uint32_t *) eng->tile_lit.ptr;
+    a.n_tiles = eng->n_tiles;
+    GSS_TRY(eng->err.reserve(sizeof(uint32_t)));
+    a.err = (uint32_t *) eng->err.ptr;
     a.start = (const uint32_t *) eng->start.ptr;
     a.solver_of_word = (const int32_t *) eng->solver_of_word.ptr;
     a.out = (gss_report *) eng->reports.ptr;
@@ -328,13 +492,23 @@ int gss_check_launch(gss_engine *eng) {
         }
     }
     GSS_CUDA_TRY(cudaMemsetAsync(a.counts, 0, sizeof(uint32_t) * a.n_parts, eng->stream));
+    GSS_CUDA_TRY(cudaMemsetAsync(a.err, 0, sizeof(uint32_t), eng->stream));
     if (ev0) GSS_CUDA_TRY(cudaEventRecord(ev0, eng->stream));
-    GSS_TRY(launch_check(a, eng->stream, eng->sm_count));
+    if (eng->state_kind == GSS_KERNEL_TILED) {
+        GSS_TRY(launch_check_tiled(a, eng->stream, eng->sm_count));
+    } else if (eng->state_kind == GSS_KERNEL_WIDE4 || eng->state_kind == GSS_KERNEL_WIDE2) {
+        GSS_TRY(launch_check_wide(a, words_per_lane(eng->state_kind), (eng->flags & GSS_VARIANT_OCCUPANCY) ? 1 : 0,
+                                  eng->stream, eng->sm_count));
+    } else {
+        GSS_TRY(launch_check(a, eng->stream, eng->sm_count));
+    }
     if (ev1) {
         GSS_CUDA_TRY(cudaEventRecord(ev1, eng->stream));
         eng->ev_pending.emplace_back(ev0, ev1);
     }
     GSS_CUDA_TRY(cudaMemcpyAsync(eng->h_counts.ptr, eng->counts.ptr, sizeof(uint32_t) * eng->n_parts,
+                                 cudaMemcpyDeviceToHost, eng->stream));
+    GSS_CUDA_TRY(cudaMemcpyAsync((uint32_t *) eng->h_counts.ptr + eng->n_parts, a.err, sizeof(uint32_t),
                                  cudaMemcpyDeviceToHost, eng->stream));
     eng->launches++;
     eng->pass_pending = true;
@@ -354,6 +528,9 @@ int gss_check_wait(gss_engine *eng, int64_t *n_reports) {
         if (hc[p] > eng->cap_per_part) overflow = true;
     }
     if (n_reports) *n_reports = total;
+    if (hc[eng->n_parts] != 0)
+        return set_error(GSS_ERR_CUDA, "a bounded wait in the check kernel gave up (flag %u); the pass is incomplete",
+                         hc[eng->n_parts]);
     if (overflow) {
         // Next automatic capacity: twice what this pass needed.
         eng->requested_cap = std::max<int64_t>(eng->requested_cap, total * 2 + eng->n_parts * 1024);

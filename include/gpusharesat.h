@@ -85,6 +85,24 @@ int gss_engine_set_timing(gss_engine *eng, int on);
  * them), and how many launches they cover. */
 int gss_engine_kernel_time(gss_engine *eng, double *total_ms, int64_t *n_launches);
 
+/* Check-kernel kinds. */
+#define GSS_KERNEL_AUTO -1   /* default: picked from the word count at gss_state_set */
+#define GSS_KERNEL_DIRECT 0  /* a lane group per clause, one 32-slot word per lane */
+#define GSS_KERNEL_TILED 1   /* clause tiles staged in shared memory by bulk copy, K clause slots */
+#define GSS_KERNEL_WIDE4 2   /* a lane group per clause, four words per lane (256-bit loads) */
+#define GSS_KERNEL_WIDE2 3   /* a lane group per clause, two words per lane (128-bit loads) */
+/* Variant flags. */
+#define GSS_VARIANT_L2_HINT 1    /* L2 evict-last policy on state loads (direct, tiled) */
+#define GSS_VARIANT_OCCUPANCY 2  /* compile-time register cap for 8 blocks per SM (wide) */
+/* Selects the check-kernel variant. A group of lanes_per_clause lanes checks
+ * one clause against a slot block of lanes_per_clause x (words per lane)
+ * 32-slot words (0 = automatic: one word per lane up to a full warp, or 32
+ * words per block for the wide kinds); `depth` = state loads in flight per
+ * lane (direct, wide) or clause slots per group (tiled); `flags` =
+ * GSS_VARIANT_*. Takes effect for the next gss_state_set (the state is laid
+ * out per slot block). */
+int gss_engine_set_variant(gss_engine *eng, int kind, int lanes_per_clause, int depth, int flags);
+
 /* ---- clause database (replaces HostClauses + DClauses,
  *      gpuShareLib/Clauses.cu:297-356 and :47-145) ---- */
 /* Replaces the database with n_clauses clauses given in CSR form on the

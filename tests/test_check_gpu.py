@@ -153,3 +153,32 @@ def test_reference_known_answers_on_gpu(engine, case):
     gpu = _gpu_reports(engine, wl)
     got = oracle.expand(gpu)
     np.testing.assert_array_equal(got, kat.expected_triples(case))
+
+
+DIRECT_VARIANTS = [(0, l, g, h) for l, gs in ((2, (1, 2)), (4, (1, 2, 4)), (8, (1, 2, 4, 8)), (16, (1, 2, 4, 8)),
+                                                (32, (1, 2, 4, 8))) for g in gs for h in (0, 1)]
+TILED_VARIANTS = [(1, l, k, h) for l in (0, 1, 2, 4, 8, 16, 32) for k in (2, 4, 8) for h in (0, 1)]
+WIDE_VARIANTS = [(kind, l, d, occ * 2) for kind, l, ds in ((2, 8, (1, 2, 4)), (2, 4, (1, 2, 4)), (2, 2, (1, 2)),
+                                                             (3, 16, (1, 2, 4)), (3, 8, (1, 2, 4)))
+                 for d in ds for occ in (0, 1)]
+
+
+@pytest.mark.parametrize("kind,lpc,depth,hints", DIRECT_VARIANTS + TILED_VARIANTS + WIDE_VARIANTS)
+def test_every_kernel_variant_matches_oracle(engine, kind, lpc, depth, hints):
+    """Each kernel variant (kind, lanes per clause, loads in flight or clause
+    slots, cache hints) is bit-exact, including slot counts that do not fill
+    the last slot block and clauses longer than a tile."""
+    wl = W.make_scale(seed=11, n_vars=2 ** 14, n_clauses=20_000, n_solvers=13)
+    # a few clauses longer than a staged tile (512 literals)
+    rng = np.random.default_rng(5)
+    extra_l, extra_o = W.distinct_var_clauses(rng, np.array([513, 700, 2000]), wl.n_vars)
+    lits = np.concatenate([wl.lits, extra_l])
+    offsets = np.concatenate([wl.offsets, wl.offsets[-1] + extra_o[1:]])
+    wl = W.Workload(wl.name, wl.n_vars, lits, offsets, wl.state, wl.start, wl.solver_of_word, wl.n_solvers)
+    ref = oracle.check(wl.lits, wl.offsets, wl.state, wl.start)
+    engine.set_variant(kind, lpc, depth, hints)
+    try:
+        gpu = _gpu_reports(engine, wl)
+    finally:
+        engine.set_variant()
+    _assert_same(gpu, ref, wl)
