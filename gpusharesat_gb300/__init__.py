@@ -204,3 +204,237 @@ def sort_reports(rep):
     """Reports in (clause, word) order, for comparison with the oracle."""
     order = np.lexsort((rep["word"], rep["clause"]))
     return rep[order]
+
+
+# ---------------------------------------------------------------- sharer ----
+
+class _SharerOptions(ctypes.Structure):
+    _fields_ = [("gpu_block_count_guideline", ctypes.c_int),
+                ("gpu_threads_per_block_guideline", ctypes.c_int),
+                ("min_gpu_latency_micros", ctypes.c_int),
+                ("verbosity", ctypes.c_int),
+                ("clause_activity_decay", ctypes.c_double),
+                ("quick_prof", ctypes.c_int),
+                ("init_report_count_per_category", ctypes.c_int),
+                ("max_page_locked_memory", ctypes.c_int)]
+
+
+_LOG_FN = ctypes.CFUNCTYPE(None, ctypes.c_char_p, ctypes.c_void_p)
+
+GLOBAL_STATS = ["gpuClauses", "gpuClauseLengthSum", "gpuClausesAdded", "gpuRuns", "clauseTestsOnGroups",
+                "clauseTestsOnAssigs", "totalAssigClauseTested", "gpuReduceDbs", "gpuReports",
+                "timeSpentTestingClauses", "timeSpentFillingAssigs", "timeSpentFillingReported",
+                "timeSpentReduceGpuDb"]
+ONE_SOLVER_STATS = ["varUpdatesSentToGpu", "assigsSentToGpu", "failuresToFindAssig", "reportedClauses",
+                    "reportedClausesUnit", "reportedClausesBinary"]
+
+
+def _sharer_sigs(lib):
+    if getattr(lib, "_gss_sharer_sigs", False):
+        return
+    c_int, c_i64, vp = ctypes.c_int, ctypes.c_int64, ctypes.c_void_p
+    ip = ctypes.POINTER(ctypes.c_int)
+    _sig(lib, "gss_sharer_options_default", None, vp)
+    _sig(lib, "gss_sharer_create", c_int, vp, _LOG_FN, vp, c_int, vp)
+    _sig(lib, "gss_sharer_destroy", c_int, vp)
+    _sig(lib, "gss_sharer_gpu_run", c_int, vp)
+    _sig(lib, "gss_sharer_reduce_db", c_int, vp)
+    _sig(lib, "gss_sharer_added_clause_count", c_i64, vp)
+    _sig(lib, "gss_sharer_added_clause_count_at_last_reduce_db", c_i64, vp)
+    _sig(lib, "gss_sharer_has_run_out_of_gpu_memory_once", c_int, vp)
+    _sig(lib, "gss_sharer_gpu_mem_info", c_int, vp, vp, vp)
+    _sig(lib, "gss_sharer_global_stat_count", c_int)
+    _sig(lib, "gss_sharer_global_stat", c_i64, vp, c_int)
+    _sig(lib, "gss_sharer_global_stat_name", ctypes.c_char_p, c_int)
+    _sig(lib, "gss_sharer_one_solver_stat_count", c_int)
+    _sig(lib, "gss_sharer_one_solver_stat_name", ctypes.c_char_p, c_int)
+    _sig(lib, "gss_sharer_one_solver_stat", c_i64, vp, c_int, c_int)
+    _sig(lib, "gss_sharer_set_var_count", c_int, vp, c_int)
+    _sig(lib, "gss_sharer_add_clause", c_i64, vp, c_int, vp, c_int)
+    _sig(lib, "gss_sharer_set_cpu_solver_count", c_int, vp, c_int)
+    _sig(lib, "gss_sharer_try_set_solver_values", c_int, vp, c_int, vp, c_int)
+    _sig(lib, "gss_sharer_unset_solver_values", c_int, vp, c_int, vp, c_int)
+    _sig(lib, "gss_sharer_try_send_assignment", c_i64, vp, c_int)
+    _sig(lib, "gss_sharer_pop_reported_clause", c_int, vp, c_int, ctypes.POINTER(ip), ip,
+         ctypes.POINTER(ctypes.c_int64))
+    _sig(lib, "gss_sharer_last_assig_all_reported", c_i64, vp, c_int)
+    _sig(lib, "gss_sharer_current_assignment", c_int, vp, c_int, vp)
+    _sig(lib, "gss_sharer_set_max_clause_len", c_int, vp, c_int)
+    _sig(lib, "gss_sharer_set_variant", c_int, vp, c_int, c_int, c_int, c_int)
+    _sig(lib, "gss_activity_create", vp, ctypes.c_float)
+    _sig(lib, "gss_activity_destroy", None, vp)
+    _sig(lib, "gss_activity_add", c_i64, vp, c_int)
+    _sig(lib, "gss_activity_bump", c_int, vp, c_i64)
+    _sig(lib, "gss_activity_decay", c_int, vp)
+    _sig(lib, "gss_activity_get", ctypes.c_float, vp, c_i64)
+    _sig(lib, "gss_activity_approx_nth", ctypes.c_float, vp, c_int, c_int, c_i64)
+    _sig(lib, "gss_activity_removing_thresholds", c_int, vp, c_int, c_i64, ip, ip, ctypes.POINTER(ctypes.c_float))
+    lib._gss_sharer_sigs = True
+
+
+def _int_array(lits):
+    a = np.ascontiguousarray(lits, dtype=np.int32)
+    return a, a.ctypes.data_as(ctypes.c_void_p)
+
+
+class ClauseSharer:
+    """The reference's GpuClauseSharer (gpuShareLib/GpuClauseSharer.h:74-163)
+    through the C ABI, with the same method names. Literals are ints,
+    2*var + sign (sign 1 = negative)."""
+
+    def __init__(self, gpuBlockCountGuideline=-1, gpuThreadsPerBlockGuideline=-1, minGpuLatencyMicros=-1,
+                 verbosity=0, clauseActivityDecay=-1.0, quickProf=True, initReportCountPerCategory=-1,
+                 maxPageLockedMemory=-1, device=0, log=None):
+        self.lib = load()
+        _sharer_sigs(self.lib)
+        o = _SharerOptions(gpuBlockCountGuideline, gpuThreadsPerBlockGuideline, minGpuLatencyMicros, verbosity,
+                           clauseActivityDecay, 1 if quickProf else 0, initReportCountPerCategory,
+                           maxPageLockedMemory)
+        self._log = _LOG_FN(lambda msg, ctx: log(msg.decode())) if log else _LOG_FN()
+        h = ctypes.c_void_p()
+        _check(self.lib.gss_sharer_create(ctypes.byref(o), self._log, None, device, ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.gss_sharer_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def gpuRun(self):
+        _check(self.lib.gss_sharer_gpu_run(self.h))
+
+    def reduceDb(self):
+        _check(self.lib.gss_sharer_reduce_db(self.h))
+
+    def getAddedClauseCount(self):
+        return int(self.lib.gss_sharer_added_clause_count(self.h))
+
+    def getAddedClauseCountAtLastReduceDb(self):
+        return int(self.lib.gss_sharer_added_clause_count_at_last_reduce_db(self.h))
+
+    def hasRunOutOfGpuMemoryOnce(self):
+        return bool(self.lib.gss_sharer_has_run_out_of_gpu_memory_once(self.h))
+
+    def getGpuMemInfo(self):
+        f, t = ctypes.c_size_t(), ctypes.c_size_t()
+        _check(self.lib.gss_sharer_gpu_mem_info(self.h, ctypes.byref(f), ctypes.byref(t)))
+        return int(f.value), int(t.value)
+
+    def getGlobalStatCount(self):
+        return int(self.lib.gss_sharer_global_stat_count())
+
+    def getGlobalStat(self, stat):
+        if isinstance(stat, str):
+            stat = GLOBAL_STATS.index(stat)
+        return int(self.lib.gss_sharer_global_stat(self.h, stat))
+
+    def getGlobalStatName(self, stat):
+        return self.lib.gss_sharer_global_stat_name(stat).decode()
+
+    def getOneSolverStatCount(self):
+        return int(self.lib.gss_sharer_one_solver_stat_count())
+
+    def getOneSolverStatName(self, stat):
+        return self.lib.gss_sharer_one_solver_stat_name(stat).decode()
+
+    def getOneSolverStat(self, solver, stat):
+        if isinstance(stat, str):
+            stat = ONE_SOLVER_STATS.index(stat)
+        return int(self.lib.gss_sharer_one_solver_stat(self.h, solver, stat))
+
+    def setVarCount(self, n):
+        _check(self.lib.gss_sharer_set_var_count(self.h, n))
+
+    def addClause(self, solverId, lits):
+        a, p = _int_array(lits)
+        return int(self.lib.gss_sharer_add_clause(self.h, solverId, p, a.shape[0]))
+
+    def setCpuSolverCount(self, n):
+        _check(self.lib.gss_sharer_set_cpu_solver_count(self.h, n))
+
+    def trySetSolverValues(self, solver, lits):
+        a, p = _int_array(lits)
+        return bool(self.lib.gss_sharer_try_set_solver_values(self.h, solver, p, a.shape[0]))
+
+    def unsetSolverValues(self, solver, lits):
+        a, p = _int_array(lits)
+        _check(self.lib.gss_sharer_unset_solver_values(self.h, solver, p, a.shape[0]))
+
+    def trySendAssignment(self, solver):
+        return int(self.lib.gss_sharer_try_send_assignment(self.h, solver))
+
+    def popReportedClause(self, solver):
+        """(list of literals, gpu clause id), or None."""
+        lp = ctypes.POINTER(ctypes.c_int)()
+        n = ctypes.c_int()
+        cid = ctypes.c_int64()
+        if not self.lib.gss_sharer_pop_reported_clause(self.h, solver, ctypes.byref(lp), ctypes.byref(n),
+                                                       ctypes.byref(cid)):
+            return None
+        return [lp[i] for i in range(n.value)], int(cid.value)
+
+    def popAll(self, solver):
+        out = []
+        while True:
+            r = self.popReportedClause(solver)
+            if r is None:
+                return out
+            out.append(r)
+
+    def getLastAssigAllReported(self, solver):
+        return int(self.lib.gss_sharer_last_assig_all_reported(self.h, solver))
+
+    def getCurrentAssignment(self, solver, n_vars):
+        buf = np.zeros(n_vars, dtype=np.uint8)
+        _check(self.lib.gss_sharer_current_assignment(self.h, solver, buf.ctypes.data_as(ctypes.c_void_p)))
+        return buf
+
+    def setMaxClauseLen(self, n):
+        _check(self.lib.gss_sharer_set_max_clause_len(self.h, n))
+
+    def setVariant(self, kind=-1, lanes_per_clause=0, depth=2, flags=0):
+        _check(self.lib.gss_sharer_set_variant(self.h, kind, lanes_per_clause, depth, flags))
+
+
+class ClauseActivity:
+    """The reduceDb policy on its own (host code, no GPU): activity with decay,
+    bump and rescale, and the removal thresholds."""
+
+    def __init__(self, decay):
+        self.lib = load()
+        _sharer_sigs(self.lib)
+        self.h = ctypes.c_void_p(self.lib.gss_activity_create(ctypes.c_float(decay)))
+
+    def __del__(self):
+        try:
+            if self.h:
+                self.lib.gss_activity_destroy(self.h)
+        except Exception:
+            pass
+
+    def add(self, lbd):
+        return int(self.lib.gss_activity_add(self.h, lbd))
+
+    def bump(self, i):
+        _check(self.lib.gss_activity_bump(self.h, i))
+
+    def decay(self):
+        _check(self.lib.gss_activity_decay(self.h))
+
+    def get(self, i):
+        return float(self.lib.gss_activity_get(self.h, i))
+
+    def approx_nth(self, min_lbd, max_lbd, n):
+        return float(self.lib.gss_activity_approx_nth(self.h, min_lbd, max_lbd, n))
+
+    def removing_thresholds(self, act_only, total):
+        a, b, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
+        _check(self.lib.gss_activity_removing_thresholds(self.h, 1 if act_only else 0, total, ctypes.byref(a),
+                                                         ctypes.byref(b), ctypes.byref(c)))
+        return int(a.value), int(b.value), float(c.value)

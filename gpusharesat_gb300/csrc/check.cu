@@ -102,7 +102,7 @@ __device__ __forceinline__ void flush_stage(gss_report *stage, uint32_t n, gss_r
 
 template <int LPC, int G>
 __global__ void __launch_bounds__(kWarps * 32) check_kernel(CheckArgs a) {
-    static_assert(LPC == 2 || LPC == 4 || LPC == 8 || LPC == 16 || LPC == 32, "lanes per clause");
+    static_assert(LPC == 1 || LPC == 2 || LPC == 4 || LPC == 8 || LPC == 16 || LPC == 32, "lanes per clause");
     static_assert(G >= 1 && G <= LPC, "prefetch depth");
     constexpr int CPW = 32 / LPC;  // clauses per warp
     __shared__ gss_report stage_all[kWarps][kStage];
@@ -417,6 +417,7 @@ int launch_check_wide(const CheckArgs &a, int wpl, int occ, cudaStream_t stream,
 
 bool valid_variant(int lpc, int g) {
     switch (lpc) {
+        case 1: return g == 1;
         case 2: return g == 1 || g == 2;
         case 4: return g == 1 || g == 2 || g == 4;
         case 8: return g == 1 || g == 2 || g == 4 || g == 8;
@@ -430,6 +431,7 @@ int launch_check(const CheckArgs &a, cudaStream_t stream, int sm_count) {
     if (a.n_clauses == 0 || a.n_blocks == 0) return GSS_OK;
 #define GSS_VARIANT(L, GG) \
     if (a.lpc == L && a.g == GG) return launch_variant<L, GG>(a, stream, sm_count);
+    GSS_VARIANT(1, 1)
     GSS_VARIANT(2, 1) GSS_VARIANT(2, 2)
     GSS_VARIANT(4, 1) GSS_VARIANT(4, 2) GSS_VARIANT(4, 4)
     GSS_VARIANT(8, 1) GSS_VARIANT(8, 2) GSS_VARIANT(8, 4) GSS_VARIANT(8, 8)

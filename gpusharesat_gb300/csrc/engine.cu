@@ -338,7 +338,9 @@ int gss_state_set(gss_engine *eng, const uint32_t *state, int64_t n_vars, int n_
             lpc = n_words >= 32 ? 8 : n_words >= 16 ? 4 : 2;
         } else {
             kind = GSS_KERNEL_DIRECT;
-            lpc = 0;
+            lpc = 1;
+            while (lpc < n_words) lpc *= 2;
+            if (lpc == 1) depth = 1;
         }
     }
     const int wpl = words_per_lane(kind);

@@ -37,6 +37,7 @@
 
 #include <stddef.h>
 #include <stdint.h>
+#include <stdio.h>
 
 #ifdef __cplusplus
 extern "C" {
@@ -147,6 +148,92 @@ int gss_check_copy_reports(gss_engine *eng, gss_report *out, int64_t cap, int64_
 int gss_check_pass_host(gss_engine *eng, const uint32_t *state, int64_t n_vars, int n_words,
                         const uint32_t *start, const int32_t *solver_of_word,
                         gss_report *out, int64_t cap, int64_t *n_reports);
+
+/* ---- the clause sharer: C form of GpuShare::GpuClauseSharer
+ *      (gpuShareLib/GpuClauseSharer.h:74-163) ---- */
+
+/* Options, field for field GpuClauseSharerOptions (gpuShareLib/GpuClauseSharer.h:25-58);
+ * -1 selects the default as there. */
+typedef struct gss_sharer_options {
+    int gpu_block_count_guideline;        /* sizes the report queues; kernels size their own grids */
+    int gpu_threads_per_block_guideline;
+    int min_gpu_latency_micros;           /* each gpu_run lasts at least this long (default 50) */
+    int verbosity;
+    double clause_activity_decay;         /* default 0.99999 */
+    int quick_prof;                       /* time the phases of a pass into the global stats */
+    int init_report_count_per_category;   /* default 10 */
+    int max_page_locked_memory;
+} gss_sharer_options;
+
+typedef struct gss_sharer gss_sharer;
+typedef void (*gss_log_fn)(const char *message, void *ctx);
+
+/* Fills *o with the defaults of GpuClauseSharerOptions() (GpuClauseSharer.h:48-57). */
+void gss_sharer_options_default(gss_sharer_options *o);
+/* makeGpuClauseSharerPtr (GpuClauseSharer.h:165); opts may be NULL (defaults),
+ * log_fn may be NULL (no log), device < 0 = the calling thread's current
+ * CUDA device. */
+int gss_sharer_create(const gss_sharer_options *opts, gss_log_fn log_fn, void *log_ctx, int device,
+                      gss_sharer **out);
+int gss_sharer_destroy(gss_sharer *s);
+
+/* Called from one thread (the GPU thread), or with locking. */
+int gss_sharer_gpu_run(gss_sharer *s);                                        /* gpuRun, :83 */
+int gss_sharer_reduce_db(gss_sharer *s);                                      /* reduceDb, :87 */
+int64_t gss_sharer_added_clause_count(gss_sharer *s);                         /* getAddedClauseCount, :90 */
+int64_t gss_sharer_added_clause_count_at_last_reduce_db(gss_sharer *s);       /* :92 */
+int gss_sharer_has_run_out_of_gpu_memory_once(gss_sharer *s);                 /* :95 */
+int gss_sharer_gpu_mem_info(gss_sharer *s, size_t *free_bytes, size_t *total_bytes);  /* :97 */
+int gss_sharer_global_stat_count(void);                                       /* :99 */
+int64_t gss_sharer_global_stat(gss_sharer *s, int stat);                      /* getGlobalStat, :101 */
+int gss_sharer_write_clauses_in_cnf(gss_sharer *s, FILE *file);               /* :103 */
+int gss_sharer_set_var_count(gss_sharer *s, int count);                       /* setVarCount, :105 */
+/* addClause (:109): returns the clause's id, or -1 when it has no literal or
+ * more than the maximum length (100 unless raised below). solver = -1 when
+ * the clause does not come from a solver. Thread safe. */
+int64_t gss_sharer_add_clause(gss_sharer *s, int solver, const int *lits, int count);
+int gss_sharer_set_cpu_solver_count(gss_sharer *s, int count);                /* :112, not thread safe */
+const char *gss_sharer_one_solver_stat_name(int stat);                        /* :118 */
+const char *gss_sharer_global_stat_name(int stat);                            /* :120 */
+int gss_sharer_one_solver_stat_count(void);                                   /* :122 */
+
+/* Per solver id: from that solver's thread, or with locking. */
+int gss_sharer_try_set_solver_values(gss_sharer *s, int solver, const int *lits, int count);  /* :129, 1 = set */
+int gss_sharer_unset_solver_values(gss_sharer *s, int solver, const int *lits, int count);    /* :134 */
+int64_t gss_sharer_try_send_assignment(gss_sharer *s, int solver);            /* :139, -1 = ring full */
+/* popReportedClause (:148): 1 and the clause when one is available, else 0.
+ * *lits belongs to the sharer and stays valid until the next pop for the same
+ * solver; the caller may reorder the literals in place (solvers do). */
+int gss_sharer_pop_reported_clause(gss_sharer *s, int solver, int **lits, int *count, int64_t *gpu_clause_id);
+int64_t gss_sharer_last_assig_all_reported(gss_sharer *s, int solver);        /* :151 */
+/* getCurrentAssignment (:155): assig[var] = 0 true, 1 false, 2 undefined. */
+int gss_sharer_current_assignment(gss_sharer *s, int solver, uint8_t *assig);
+int64_t gss_sharer_one_solver_stat(gss_sharer *s, int solver, int stat);     /* :159 */
+
+/* Extensions without a counterpart in GpuClauseSharer: raise the longest
+ * accepted clause (up to gss_max_clause_len()), pick the check kernel. */
+int gss_sharer_set_max_clause_len(gss_sharer *s, int n);
+int gss_sharer_set_variant(gss_sharer *s, int kind, int lanes_per_clause, int depth, int flags);
+
+/* ---- the reduceDb policy on its own (host only, no GPU needed) ----
+ * Clause activity with decay, bump and rescale, and the thresholds a reduceDb
+ * uses (gpuShareLib/Clauses.cu:231-291, 377-417, 488-525). The sharer's
+ * reduceDb runs the same code; this handle exposes it for callers and tests. */
+typedef struct gss_activity gss_activity;
+gss_activity *gss_activity_create(float decay);
+void gss_activity_destroy(gss_activity *a);
+/* Decays the increment, then adds an entry with that activity; returns its index. */
+int64_t gss_activity_add(gss_activity *a, int lbd);
+int gss_activity_bump(gss_activity *a, int64_t i);
+int gss_activity_decay(gss_activity *a);
+float gss_activity_get(const gss_activity *a, int64_t i);
+/* Upper bound of the log bucket holding the n-th lowest activity among
+ * entries with min_lbd <= lbd < max_lbd (approxNthAct). */
+float gss_activity_approx_nth(const gss_activity *a, int min_lbd, int max_lbd, int64_t n);
+/* getRemovingLbdAndAct for `total` clauses: keep lbd < *min_lim, or
+ * lbd < *max_lim with activity >= *act. */
+int gss_activity_removing_thresholds(const gss_activity *a, int act_only, int64_t total, int *min_lim, int *max_lim,
+                                     float *act);
 
 #ifdef __cplusplus
 }

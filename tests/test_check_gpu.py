@@ -155,7 +155,7 @@ def test_reference_known_answers_on_gpu(engine, case):
     np.testing.assert_array_equal(got, kat.expected_triples(case))
 
 
-DIRECT_VARIANTS = [(0, l, g, h) for l, gs in ((2, (1, 2)), (4, (1, 2, 4)), (8, (1, 2, 4, 8)), (16, (1, 2, 4, 8)),
+DIRECT_VARIANTS = [(0, l, g, h) for l, gs in ((1, (1,)), (2, (1, 2)), (4, (1, 2, 4)), (8, (1, 2, 4, 8)), (16, (1, 2, 4, 8)),
                                                 (32, (1, 2, 4, 8))) for g in gs for h in (0, 1)]
 TILED_VARIANTS = [(1, l, k, h) for l in (0, 1, 2, 4, 8, 16, 32) for k in (2, 4, 8) for h in (0, 1)]
 WIDE_VARIANTS = [(kind, l, d, occ * 2) for kind, l, ds in ((2, 8, (1, 2, 4)), (2, 4, (1, 2, 4)), (2, 2, (1, 2)),
