@@ -151,9 +151,30 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def shard_seed(rank):
+    """Each rank checks its own clause shard of the same size (weak scaling)."""
+    return 1 + 1000 * rank
+
+
 def make_workload(args, rank):
     from gpusharesat_gb300 import workloads as W
-    return W.make_scale(seed=1 + 1000 * rank, n_vars=2 ** args.vars_log2, n_clauses=args.clauses)
+    return W.make_scale(seed=shard_seed(rank), n_vars=2 ** args.vars_log2, n_clauses=args.clauses)
+
+
+def max_over_ranks(value, world, device):
+    """The slowest rank's value (all_reduce MAX over the process group)."""
+    if world == 1:
+        return float(value)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(units_per_rank_per_step, world, max_seconds_per_step):
+    """Whole-job units/s: all ranks' units over the slowest rank's time."""
+    return units_per_rank_per_step * world / max_seconds_per_step
 
 
 def cpu_baseline(wl, seconds, threads=None):
@@ -272,15 +293,11 @@ def run_gpu(args):
     eng.set_timing(False)
     n_last = eng.wait()
     assert n_last == n_reports, (n_last, n_reports)
-    elapsed_ms = ev0.elapsed_time(ev1)
     kern_ms, kern_n = eng.kernel_time()
-    t = torch.tensor([elapsed_ms], device="cuda")
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    elapsed_ms = float(t.item())
+    elapsed_ms = max_over_ranks(ev0.elapsed_time(ev1), world, "cuda")
     ms_per_step = elapsed_ms / args.steps
     checks_per_pass = wl.n_clauses * wl.n_assignments
-    value = checks_per_pass * world / (ms_per_step / 1e3)
+    value = job_throughput(checks_per_pass, world, ms_per_step / 1e3)
 
     # ---- end to end through host buffers (e2e) ----
     state_h = torch.from_numpy(wl.state.reshape(-1)).pin_memory()
@@ -304,11 +321,7 @@ def run_gpu(args):
     for _ in range(args.e2e_steps):
         e2e_step()
     torch.cuda.synchronize()
-    e2e_s = (time.perf_counter() - t0) / args.e2e_steps
-    te = torch.tensor([e2e_s], device="cuda")
-    if world > 1:
-        dist.all_reduce(te, op=dist.ReduceOp.MAX)
-    e2e_s = float(te.item())
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / args.e2e_steps, world, "cuda")
     assert nrep.value == n_reports
     h2d = wl.state.nbytes + wl.start.nbytes + wl.solver_of_word.nbytes
     d2h = n_reports * 16 + 16 * 4
@@ -329,7 +342,7 @@ def run_gpu(args):
             "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded)",
             "config": config_dict(args, world),
             "reports_per_pass": n_reports,
-            "e2e": {"value": checks_per_pass * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
+            "e2e": {"value": job_throughput(checks_per_pass, world, e2e_s), "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3},
             "roofline": roofline,
             "gpu_launches": gpu_launches,
