@@ -95,12 +95,16 @@ def load_peaks():
 
 
 def load_traffic():
-    """Per-launch DRAM bytes of the check kernel from the committed ncu summary
-    (scaled to this workload there), or None."""
-    path = os.path.join(ROOT, "profiles", "check_kernel_traffic.json")
+    """Per-launch DRAM bytes (read + write) of the check kernel on this
+    workload, from the committed ncu summary (its `traffic_bytes_per_launch`
+    line), or None."""
+    import re
+    path = os.path.join(ROOT, "profiles", "check_wide_kernel_plain_scale.md")
     if os.path.exists(path):
         with open(path) as f:
-            return json.load(f).get("dram_bytes_per_launch")
+            m = re.search(r"traffic_bytes_per_launch:\s*([0-9]+)", f.read())
+            if m:
+                return int(m.group(1))
     return None
 
 

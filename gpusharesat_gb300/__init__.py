@@ -28,6 +28,7 @@ KERNEL_WIDE4 = 2
 KERNEL_WIDE2 = 3
 VARIANT_L2_HINT = 1
 VARIANT_OCCUPANCY = 2
+VARIANT_PIPELINED = 4
 
 REPORT_DTYPE = np.dtype([("clause", "<u4"), ("word", "<u4"), ("mask", "<u4"), ("solver", "<u4")])
 

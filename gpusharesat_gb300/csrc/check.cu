@@ -34,6 +34,10 @@
 // The reference does one atomicAdd per report and drops reports when a
 // category is full (Reporter.cuh:41-49); here nothing is dropped: a full
 // partition keeps counting, so the host sees the overflow and runs again.
+#include <string.h>
+
+#include <mutex>
+
 #include "common.h"
 
 namespace gss {
@@ -335,6 +339,160 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) check_wide_kernel(CheckArgs
     if (nstaged) flush_stage(stage, nstaged, out, counter, a.cap_per_part, lane);
 }
 
+// Pipelined wide variant: the same schedule and rule as check_wide_kernel,
+// with the loads a clause waits on before its first state gather moved off
+// its critical path. The next task's offsets are loaded when a task starts,
+// its first literal chunk after the task's first gather round, and a long
+// clause's next chunk while its current chunk is being checked. All these
+// loads are in bounds (guarded like the ones they replace) and at most one
+// chunk ahead.
+template <int WPL, int LPC, int G, int MINB>
+__global__ void __launch_bounds__(kWarps * 32, MINB) check_wide_pf_kernel(CheckArgs a) {
+    constexpr int CPW = 32 / LPC;
+    constexpr int BW = WPL * LPC;
+    static_assert(G >= 1 && G <= LPC, "depth");
+    __shared__ gss_report stage_all[kWarps][kStage];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int sub = lane % LPC;
+    const int grp = lane / LPC;
+    const int gbase = grp * LPC;
+    gss_report *stage = stage_all[wib];
+    const uint32_t part = blockIdx.x % a.n_parts;
+    gss_report *out = a.out + (size_t) part * a.cap_per_part;
+    uint32_t *counter = a.counts + part;
+    uint32_t nstaged = 0;
+
+    const uint32_t n_groups = (a.n_clauses + CPW - 1) / CPW;
+    const uint64_t n_tasks = (uint64_t) n_groups * a.n_blocks;
+    const uint64_t stride = (uint64_t) gridDim.x * kWarps;
+    uint64_t task = (uint64_t) blockIdx.x * kWarps + wib;
+
+    // clause of this lane's group for a task
+    auto clause_of = [&](uint64_t t) -> uint32_t {
+        const uint32_t b = (uint32_t) (t / n_groups);
+        return (uint32_t) (t - (uint64_t) b * n_groups) * CPW + grp;
+    };
+    // prefetched: offsets and first literal chunk of the current task
+    uint32_t nx_pos = 0, nx_end = 0;
+    int32_t nx_chunk = 0;
+    if (task < n_tasks) {
+        const uint32_t c0 = clause_of(task);
+        if (c0 < a.n_clauses) {
+            nx_pos = (uint32_t) __ldg(a.offsets + c0);
+            nx_end = (uint32_t) __ldg(a.offsets + c0 + 1);
+            nx_chunk = (nx_pos + sub < nx_end) ? __ldg(a.lits + nx_pos + sub) : 0;
+        }
+    }
+    for (; task < n_tasks; task += stride) {
+        const uint32_t blk = (uint32_t) (task / n_groups);
+        const uint32_t c = clause_of(task);
+        const bool valid = c < a.n_clauses;
+        const uint32_t w0 = blk * BW + sub * WPL;
+        uint32_t af[WPL], ou[WPL];
+#pragma unroll
+        for (int j = 0; j < WPL; j++) {
+            af[j] = valid ? __ldg(a.start + w0 + j) : 0u;
+            ou[j] = 0u;
+        }
+        uint32_t pos = valid ? nx_pos : 0u, end = valid ? nx_end : 0u;
+        int32_t chunk = valid ? nx_chunk : 0;
+        // start the next task's offsets now
+        const uint64_t nt = task + stride;
+        const uint32_t nc = nt < n_tasks ? clause_of(nt) : 0xFFFFFFFFu;
+        const bool nvalid = nt < n_tasks && nc < a.n_clauses;
+        nx_pos = nvalid ? (uint32_t) __ldg(a.offsets + nc) : 0u;
+        nx_end = nvalid ? (uint32_t) __ldg(a.offsets + nc + 1) : 0u;
+        bool next_chunk_due = true;
+        const uint2 *rows = a.state + (size_t) blk * a.n_vars * BW + sub * WPL;
+        while (true) {
+            bool alive = false;
+#pragma unroll
+            for (int j = 0; j < WPL; j++) alive |= (af[j] | ou[j]) != 0u;
+            if (!__any_sync(kFull, alive && pos < end)) break;
+            // this clause's next chunk, while the current one is checked
+            const int32_t after = (pos + LPC + sub < end) ? __ldg(a.lits + pos + LPC + sub) : 0;
+            const int navail = (int) min((uint32_t) LPC, end > pos ? end - pos : 0u);
+#pragma unroll 1
+            for (int k0 = 0; k0 < LPC; k0 += G) {
+                alive = false;
+#pragma unroll
+                for (int j = 0; j < WPL; j++) alive |= (af[j] | ou[j]) != 0u;
+                if (!__any_sync(kFull, alive && k0 < navail)) break;
+                uint32_t lit[G];
+                Row<WPL> st[G];
+#pragma unroll
+                for (int i = 0; i < G; i++) lit[i] = (uint32_t) __shfl_sync(kFull, chunk, gbase + k0 + i);
+#pragma unroll
+                for (int i = 0; i < G; i++) {
+#pragma unroll
+                    for (int q = 0; q < 2 * WPL; q++) st[i].v[q] = 0u;
+                    if (alive && k0 + i < navail) ld_row<WPL>(rows + (size_t) (lit[i] >> 1) * BW, st[i]);
+                }
+                if (next_chunk_due) {
+                    // the next task's offsets have had a gather round to arrive
+                    nx_chunk = (nvalid && nx_pos + sub < nx_end) ? __ldg(a.lits + nx_pos + sub) : 0;
+                    next_chunk_due = false;
+                }
+#pragma unroll
+                for (int i = 0; i < G; i++) {
+                    if (k0 + i < navail) {
+                        const bool neg = (lit[i] & 1u) != 0u;
+#pragma unroll
+                        for (int j = 0; j < WPL; j++) {
+                            const uint32_t d = st[i].v[2 * j], t = st[i].v[2 * j + 1];
+                            const uint32_t f = (neg ? t : ~t) & d;
+                            ou[j] = (af[j] & ~d) | (ou[j] & f);
+                            af[j] &= f;
+                        }
+                    }
+                }
+            }
+            pos += LPC;
+            chunk = after;
+        }
+        if (next_chunk_due) nx_chunk = (nvalid && nx_pos + sub < nx_end) ? __ldg(a.lits + nx_pos + sub) : 0;
+#pragma unroll
+        for (int j = 0; j < WPL; j++) {
+            const uint32_t rep = af[j] | ou[j];
+            const unsigned bal = __ballot_sync(kFull, rep != 0u);
+            if (bal) {
+                if (nstaged + 32 > (uint32_t) kStage) {
+                    flush_stage(stage, nstaged, out, counter, a.cap_per_part, lane);
+                    nstaged = 0;
+                }
+                if (rep) {
+                    gss_report r;
+                    r.clause = __ldg(a.orig + c);
+                    r.word = w0 + j;
+                    r.mask = rep;
+                    r.solver = (uint32_t) __ldg(a.solver_of_word + w0 + j);
+                    stage[nstaged + __popc(bal & lanemask_lt())] = r;
+                }
+                nstaged += __popc(bal);
+            }
+        }
+    }
+    if (nstaged) flush_stage(stage, nstaged, out, counter, a.cap_per_part, lane);
+}
+
+template <int WPL, int LPC, int G, int MINB>
+int launch_wide_pf_variant(const CheckArgs &a, cudaStream_t stream, int sm_count) {
+    int per_sm = 0;
+    GSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, check_wide_pf_kernel<WPL, LPC, G, MINB>,
+                                                               kWarps * 32, 0));
+    if (per_sm < 1) per_sm = 1;
+    constexpr int CPW = 32 / LPC;
+    const uint64_t n_tasks = (uint64_t) ((a.n_clauses + CPW - 1) / CPW) * a.n_blocks;
+    uint64_t blocks = (uint64_t) sm_count * per_sm;
+    const uint64_t need = (n_tasks + kWarps - 1) / kWarps;
+    if (blocks > need) blocks = need;
+    if (blocks < 1) blocks = 1;
+    check_wide_pf_kernel<WPL, LPC, G, MINB><<<(unsigned) blocks, kWarps * 32, 0, stream>>>(a);
+    GSS_CUDA_TRY(cudaGetLastError());
+    return GSS_OK;
+}
+
 template <int WPL, int LPC, int G, int MINB>
 int launch_wide_variant(const CheckArgs &a, cudaStream_t stream, int sm_count) {
     int per_sm = 0;
@@ -395,6 +553,27 @@ bool valid_wide_variant(int wpl, int lpc, int g, int occ) {
     if (wpl == 2 && lpc == 16) return g == 1 || g == 2 || g == 4;
     if (wpl == 2 && lpc == 8) return g == 1 || g == 2 || g == 4;
     if (wpl == 1 && lpc == 32) return g == 1 || g == 2 || g == 4;
+    return false;
+}
+
+int launch_check_wide_pf(const CheckArgs &a, int wpl, int occ, cudaStream_t stream, int sm_count) {
+    if (a.n_clauses == 0 || a.n_blocks == 0) return GSS_OK;
+#define GSS_PV(W, L, GG)                                                                      \
+    if (wpl == W && a.lpc == L && a.g == GG)                                                  \
+        return occ ? launch_wide_pf_variant<W, L, GG, 4>(a, stream, sm_count)                 \
+                   : launch_wide_pf_variant<W, L, GG, 1>(a, stream, sm_count);
+    GSS_PV(4, 8, 1) GSS_PV(4, 8, 2) GSS_PV(4, 8, 4)
+    GSS_PV(4, 4, 2) GSS_PV(4, 4, 4)
+    GSS_PV(2, 16, 2) GSS_PV(2, 16, 4)
+#undef GSS_PV
+    return set_error(GSS_ERR_INVALID, "no pipelined wide kernel variant for %d words per lane, %d lanes, depth %d",
+                     wpl, a.lpc, a.g);
+}
+
+bool valid_wide_pf_variant(int wpl, int lpc, int g) {
+    if (wpl == 4 && lpc == 8) return g == 1 || g == 2 || g == 4;
+    if (wpl == 4 && lpc == 4) return g == 2 || g == 4;
+    if (wpl == 2 && lpc == 16) return g == 2 || g == 4;
     return false;
 }
 

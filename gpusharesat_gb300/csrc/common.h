@@ -91,6 +91,9 @@ int launch_check(const CheckArgs &a, cudaStream_t stream, int sm_count);
 bool valid_variant(int lpc, int g);
 int launch_check_tiled(const CheckArgs &a, cudaStream_t stream, int sm_count);
 int launch_check_wide(const CheckArgs &a, int wpl, int occ, cudaStream_t stream, int sm_count);
+// Pipelined wide kernel (occ: 4 blocks per SM register cap).
+int launch_check_wide_pf(const CheckArgs &a, int wpl, int occ, cudaStream_t stream, int sm_count);
+bool valid_wide_pf_variant(int wpl, int lpc, int g);
 bool valid_wide_variant(int wpl, int lpc, int g, int occ);
 bool valid_tiled_variant(int lpc, int k);
 

@@ -418,7 +418,8 @@ int gss_engine_set_variant(gss_engine *eng, int kind, int lanes_per_clause, int 
     } else if (kind == GSS_KERNEL_WIDE4 || kind == GSS_KERNEL_WIDE2) {
         const int wpl = words_per_lane(kind);
         const int l = lanes_per_clause ? lanes_per_clause : 32 / wpl;
-        if (!valid_wide_variant(wpl, l, depth, (flags & GSS_VARIANT_OCCUPANCY) ? 1 : 0))
+        if ((flags & GSS_VARIANT_PIPELINED) ? !valid_wide_pf_variant(wpl, l, depth)
+                                            : !valid_wide_variant(wpl, l, depth, (flags & GSS_VARIANT_OCCUPANCY) ? 1 : 0))
             return set_error(GSS_ERR_INVALID, "no wide kernel variant for %d words per lane, %d lanes, depth %d", wpl,
                              l, depth);
     } else if (kind == GSS_KERNEL_DIRECT) {
@@ -498,6 +499,10 @@ int gss_check_launch(gss_engine *eng) {
     if (ev0) GSS_CUDA_TRY(cudaEventRecord(ev0, eng->stream));
     if (eng->state_kind == GSS_KERNEL_TILED) {
         GSS_TRY(launch_check_tiled(a, eng->stream, eng->sm_count));
+    } else if ((eng->state_kind == GSS_KERNEL_WIDE4 || eng->state_kind == GSS_KERNEL_WIDE2) &&
+               (eng->flags & GSS_VARIANT_PIPELINED)) {
+        GSS_TRY(launch_check_wide_pf(a, words_per_lane(eng->state_kind), (eng->flags & GSS_VARIANT_OCCUPANCY) ? 1 : 0,
+                                     eng->stream, eng->sm_count));
     } else if (eng->state_kind == GSS_KERNEL_WIDE4 || eng->state_kind == GSS_KERNEL_WIDE2) {
         GSS_TRY(launch_check_wide(a, words_per_lane(eng->state_kind), (eng->flags & GSS_VARIANT_OCCUPANCY) ? 1 : 0,
                                   eng->stream, eng->sm_count));

@@ -94,7 +94,8 @@ int gss_engine_kernel_time(gss_engine *eng, double *total_ms, int64_t *n_launche
 #define GSS_KERNEL_WIDE2 3   /* a lane group per clause, two words per lane (128-bit loads) */
 /* Variant flags. */
 #define GSS_VARIANT_L2_HINT 1    /* L2 evict-last policy on state loads (direct, tiled) */
-#define GSS_VARIANT_OCCUPANCY 2  /* compile-time register cap for 8 blocks per SM (wide) */
+#define GSS_VARIANT_OCCUPANCY 2  /* compile-time register cap: 8 blocks per SM (wide), 4 (pipelined wide) */
+#define GSS_VARIANT_PIPELINED 4  /* wide kinds: next clause's offsets and literals loaded ahead */
 /* Selects the check-kernel variant. A group of lanes_per_clause lanes checks
  * one clause against a slot block of lanes_per_clause x (words per lane)
  * 32-slot words (0 = automatic: one word per lane up to a full warp, or 32

@@ -161,9 +161,11 @@ TILED_VARIANTS = [(1, l, k, h) for l in (0, 1, 2, 4, 8, 16, 32) for k in (2, 4, 
 WIDE_VARIANTS = [(kind, l, d, occ * 2) for kind, l, ds in ((2, 8, (1, 2, 4)), (2, 4, (1, 2, 4)), (2, 2, (1, 2)),
                                                              (3, 16, (1, 2, 4)), (3, 8, (1, 2, 4)))
                  for d in ds for occ in (0, 1)]
+PIPELINED_VARIANTS = [(kind, l, d, 4 | occ * 2) for kind, l, ds in ((2, 8, (1, 2, 4)), (2, 4, (2, 4)), (3, 16, (2, 4)))
+                      for d in ds for occ in (0, 1)]
 
 
-@pytest.mark.parametrize("kind,lpc,depth,hints", DIRECT_VARIANTS + TILED_VARIANTS + WIDE_VARIANTS)
+@pytest.mark.parametrize("kind,lpc,depth,hints", DIRECT_VARIANTS + TILED_VARIANTS + WIDE_VARIANTS + PIPELINED_VARIANTS)
 def test_every_kernel_variant_matches_oracle(engine, kind, lpc, depth, hints):
     """Each kernel variant (kind, lanes per clause, loads in flight or clause
     slots, cache hints) is bit-exact, including slot counts that do not fill
