@@ -238,7 +238,8 @@ __device__ __forceinline__ void ld_row<4>(const uint2 *p, Row<4> &r) {
         : "l"(p));
 }
 
-template <int WPL, int LPC, int G, int MINB>
+// MAP_IDS = false: reports carry the clause's CSR index itself (a.orig unused).
+template <int WPL, int LPC, int G, int MINB, bool MAP_IDS = true>
 __global__ void __launch_bounds__(kWarps * 32, MINB) check_wide_kernel(CheckArgs a) {
     constexpr int CPW = 32 / LPC;
     constexpr int BW = WPL * LPC;
@@ -326,7 +327,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) check_wide_kernel(CheckArgs
                 }
                 if (rep) {
                     gss_report r;
-                    r.clause = __ldg(a.orig + c);
+                    r.clause = MAP_IDS ? __ldg(a.orig + c) : c;
                     r.word = w0 + j;
                     r.mask = rep;
                     r.solver = (uint32_t) __ldg(a.solver_of_word + w0 + j);
@@ -493,10 +494,10 @@ int launch_wide_pf_variant(const CheckArgs &a, cudaStream_t stream, int sm_count
     return GSS_OK;
 }
 
-template <int WPL, int LPC, int G, int MINB>
+template <int WPL, int LPC, int G, int MINB, bool MAP_IDS = true>
 int launch_wide_variant(const CheckArgs &a, cudaStream_t stream, int sm_count) {
     int per_sm = 0;
-    GSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, check_wide_kernel<WPL, LPC, G, MINB>,
+    GSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, check_wide_kernel<WPL, LPC, G, MINB, MAP_IDS>,
                                                                kWarps * 32, 0));
     if (per_sm < 1) per_sm = 1;
     constexpr int CPW = 32 / LPC;
@@ -505,7 +506,7 @@ int launch_wide_variant(const CheckArgs &a, cudaStream_t stream, int sm_count) {
     const uint64_t need = (n_tasks + kWarps - 1) / kWarps;
     if (blocks > need) blocks = need;
     if (blocks < 1) blocks = 1;
-    check_wide_kernel<WPL, LPC, G, MINB><<<(unsigned) blocks, kWarps * 32, 0, stream>>>(a);
+    check_wide_kernel<WPL, LPC, G, MINB, MAP_IDS><<<(unsigned) blocks, kWarps * 32, 0, stream>>>(a);
     GSS_CUDA_TRY(cudaGetLastError());
     return GSS_OK;
 }
@@ -633,3 +634,92 @@ int launch_relayout(const uint2 *src, uint2 *dst, uint32_t n_vars, uint32_t n_wo
 }
 
 }  // namespace gss
+
+// ------------------------------------------------ allocation-free pass ----
+//
+// gss_check_noalloc: the wide check kernel for callers that cannot allocate
+// device memory. The kernel's only working memory is its report reservation
+// counters (one per output partition); here they live in a fixed,
+// file-scope device array instead of a cudaMalloc'ed buffer, so the call
+// allocates nothing. Every GPU that loads this library holds the array
+// (256 bytes) until the process exits.
+
+namespace {
+
+constexpr uint32_t kNoAllocMaxParts = 64;
+constexpr int kNoAllocMaxDevices = 64;
+
+// Report reservation counters of gss_check_noalloc, shared by all its calls.
+static __device__ __align__(256) uint32_t g_noalloc_counters[kNoAllocMaxParts];
+
+std::mutex g_noalloc_lock;
+void *g_noalloc_addr[kNoAllocMaxDevices];  // device address of the counters, per device
+
+// The counters' device address on the current device. In host code the
+// array's name is only a host-side stand-in; the first call on a device asks
+// the runtime for the real address and keeps it.
+int noalloc_counters(uint32_t **out) {
+    int dev = 0;
+    GSS_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices)
+        return gss::set_error(GSS_ERR_INVALID, "device %d: the allocation-free pass supports devices 0..%d", dev,
+                              kNoAllocMaxDevices - 1);
+    std::lock_guard<std::mutex> g(g_noalloc_lock);
+    if (!g_noalloc_addr[dev]) {
+        void *p = nullptr;
+        GSS_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_counters));
+        g_noalloc_addr[dev] = p;
+    }
+    *out = (uint32_t *) g_noalloc_addr[dev];
+    return GSS_OK;
+}
+
+}  // namespace
+
+extern "C" int gss_check_noalloc(const int32_t *lits, const int64_t *offsets, uint32_t n_clauses,
+                                 const uint32_t *state, uint32_t n_vars, uint32_t n_blocks, const uint32_t *start,
+                                 const int32_t *solver_of_word, gss_report *out, uint32_t n_parts,
+                                 uint32_t cap_per_part, uint32_t *counts_out, void *stream) {
+    using namespace gss;
+    if (n_parts == 0 || n_parts > kNoAllocMaxParts)
+        return set_error(GSS_ERR_INVALID,
+                         "gss_check_noalloc: %u report partitions requested; the allocation-free pass has a fixed "
+                         "array of %u counters",
+                         n_parts, kNoAllocMaxParts);
+    if (!counts_out || (n_clauses > 0 && (!lits || !offsets)) || (n_blocks > 0 && (!state || !start ||
+                                                                                  !solver_of_word)) ||
+        (cap_per_part > 0 && !out))
+        return set_error(GSS_ERR_INVALID, "gss_check_noalloc: NULL input or output");
+    if ((uint64_t) cap_per_part * n_parts > 0xFFFFFFFFull)
+        return set_error(GSS_ERR_INVALID, "gss_check_noalloc: output capacity above 2^32 records");
+    cudaStream_t st = (cudaStream_t) stream;
+    uint32_t *counters = nullptr;
+    GSS_TRY(noalloc_counters(&counters));
+    // every call starts from zeroed counters: they keep the previous call's values
+    GSS_CUDA_TRY(cudaMemsetAsync(counters, 0, n_parts * sizeof(uint32_t), st));
+    if (n_clauses > 0 && n_blocks > 0) {
+        int dev = 0, sms = 0;
+        GSS_CUDA_TRY(cudaGetDevice(&dev));
+        GSS_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        CheckArgs a;
+        memset(&a, 0, sizeof a);
+        a.lits = lits;
+        a.offsets = offsets;
+        a.orig = nullptr;
+        a.n_clauses = n_clauses;
+        a.state = (const uint2 *) state;
+        a.n_vars = n_vars;
+        a.n_blocks = n_blocks;
+        a.start = start;
+        a.solver_of_word = solver_of_word;
+        a.out = out;
+        a.counts = counters;
+        a.n_parts = n_parts;
+        a.cap_per_part = cap_per_part;
+        a.lpc = 8;
+        a.g = 2;
+        GSS_TRY((launch_wide_variant<4, 8, 2, 1, false>(a, st, sms)));
+    }
+    GSS_CUDA_TRY(cudaMemcpyAsync(counts_out, counters, n_parts * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st));
+    return GSS_OK;
+}

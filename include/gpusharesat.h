@@ -150,6 +150,35 @@ int gss_check_pass_host(gss_engine *eng, const uint32_t *state, int64_t n_vars, 
                         const uint32_t *start, const int32_t *solver_of_word,
                         gss_report *out, int64_t cap, int64_t *n_reports);
 
+/* ---- allocation-free check pass ----
+ * No counterpart in the reference. For callers that cannot allocate device
+ * memory: a solver process that hands its whole GPU budget to its own pool at
+ * start-up (a cudaMalloc would then fail or break that budget), or a
+ * latency-bound loop that must not stall in the allocator, which can
+ * synchronize the device. The caller passes every input and output as device
+ * pointers; the call allocates nothing and only queues work on `stream`
+ * (NULL = the default stream): it returns before the pass ends.
+ *
+ * Inputs: the CSR clause database (lits, offsets[n_clauses + 1]); the
+ * assignment words in the wide layout, state[n_blocks][n_vars][32][2] =
+ * {isDef, isTrue} for words 32*b .. 32*b + 31 (pad past the last word with
+ * zeros), start[n_blocks * 32] and solver_of_word[n_blocks * 32].
+ * Outputs: out[n_parts * cap_per_part] report records, partition p holding
+ * min(counts_out[p], cap_per_part) records from out + p * cap_per_part, with
+ * `clause` the CSR index; counts_out[n_parts]. A count above cap_per_part
+ * means that partition overflowed: run again with more room.
+ * Limit: n_parts <= 64. The kernel's reservation counters live in one fixed
+ * 256-byte device array, which every GPU that loads this library keeps until
+ * the process exits, and which all calls share: overlapping calls on the GPU
+ * race and give wrong counts. Each call clears the counters first (they keep
+ * the previous call's values). The first call on a device looks up the
+ * array's device address; make that first call before any stream capture.
+ * The results are the same as gss_check_launch's with the GSS_KERNEL_WIDE4
+ * variant (8 lanes per clause, depth 2). */
+int gss_check_noalloc(const int32_t *lits, const int64_t *offsets, uint32_t n_clauses, const uint32_t *state,
+                      uint32_t n_vars, uint32_t n_blocks, const uint32_t *start, const int32_t *solver_of_word,
+                      gss_report *out, uint32_t n_parts, uint32_t cap_per_part, uint32_t *counts_out, void *stream);
+
 /* ---- the clause sharer: C form of GpuShare::GpuClauseSharer
  *      (gpuShareLib/GpuClauseSharer.h:74-163) ---- */
 
