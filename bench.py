@@ -8,9 +8,10 @@ those shapes (the reference publishes no dataset).
 
 value: checks/s with the clause database and the assignment planes resident
        in HBM (kernel passes back to back, CUDA events on the launch stream).
-e2e:   the same metric through the C ABI call gss_check_pass_host with host
-       buffers: per step the assignment planes go host->device from pinned
-       memory and the reports come back device->host.
+e2e:   the same metric through the C ABI call gss_check_passes_host with host
+       buffers: every step's assignment planes go host->device from pinned
+       memory and its reports come back device->host; the copies of
+       neighbouring steps overlap the current step's check.
 The inputs (about 0.6 GB) are larger than the 129 MB L2, so no flush is
 needed between steps.
 
@@ -37,7 +38,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "clause x assignment checks/s (bit-exact, plain check at scale)"
+METRIC = "clause\u00d7assignment checks/s on 1 GB300, bit-exact"
 UNIT = "checks/s"
 
 
@@ -47,9 +48,11 @@ def parse():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--clauses", type=int, default=4_000_000)
+    p.add_argument("--workload", default="scale", choices=["scale", "small"],
+                   help="scale: 4e6 clauses x 1024 assignments (the headline); small: 1e5 clauses x 64 assignments")
+    p.add_argument("--clauses", type=int, default=None)
     p.add_argument("--vars-log2", type=int, default=20)
-    p.add_argument("--e2e-steps", type=int, default=5)
+    p.add_argument("--e2e-steps", type=int, default=10)
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--kind", type=int, default=None, help="check kernel kind (0 direct, 1 tiled)")
@@ -67,6 +70,14 @@ def dist_env():
 
 
 def config_dict(args, world):
+    if args.workload == "small":
+        return {
+            "workload": "plain check, small: %d clauses (lengths 2-30, geometric mean 8) x 64 assignments "
+                        "(1 solver), 2^14 variables, 1%% planted reports" % args.clauses,
+            "clauses_per_gpu": args.clauses, "assignments": 64, "variables": 2 ** 14, "solvers": 1,
+            "l2": "inputs fit in L2 (about 4 MB): no roofline claim",
+            "parallelism": "clause shards, %d replica(s)" % world,
+        }
     return {
         "workload": "plain check at scale: %d clauses (lengths 2-100) x 1024 assignments (32 solvers x 32), "
                     "2^%d variables, 0.1%% planted reports" % (args.clauses, args.vars_log2),
@@ -162,6 +173,8 @@ def shard_seed(rank):
 
 def make_workload(args, rank):
     from gpusharesat_gb300 import workloads as W
+    if args.workload == "small":
+        return W.make_small(seed=shard_seed(rank) - 1, n_clauses=args.clauses)
     return W.make_scale(seed=shard_seed(rank), n_vars=2 ** args.vars_log2, n_clauses=args.clauses)
 
 
@@ -304,29 +317,33 @@ def run_gpu(args):
     value = job_throughput(checks_per_pass, world, ms_per_step / 1e3)
 
     # ---- end to end through host buffers (e2e) ----
-    state_h = torch.from_numpy(wl.state.reshape(-1)).pin_memory()
+    # gss_check_passes_host: K passes in one call, each copying its state in
+    # from pinned host memory and its reports out to pinned host memory, the
+    # copies of neighbouring passes overlapping the check of the current one.
+    states_h = [torch.from_numpy(wl.state.reshape(-1)).pin_memory() for _ in range(2)]
     start_h = torch.from_numpy(wl.start).pin_memory()
     sow_h = torch.from_numpy(wl.solver_of_word).pin_memory()
-    out_h = torch.empty((n_reports + 1024) * 4, dtype=torch.int32).pin_memory()
+    cap = n_reports + 1024
+    outs_h = [torch.empty(cap * 4, dtype=torch.int32).pin_memory() for _ in range(2)]
     lib = g.load()
-    nrep = ctypes.c_int64()
 
-    def e2e_step():
-        rc = lib.gss_check_pass_host(eng.h, ctypes.c_void_p(state_h.data_ptr()), wl.n_vars, wl.n_words,
-                                     ctypes.c_void_p(start_h.data_ptr()), ctypes.c_void_p(sow_h.data_ptr()),
-                                     ctypes.c_void_p(out_h.data_ptr()), n_reports + 1024, ctypes.byref(nrep))
+    def e2e_run(k):
+        sp = (ctypes.c_void_p * k)(*[states_h[i % 2].data_ptr() for i in range(k)])
+        op = (ctypes.c_void_p * k)(*[outs_h[i % 2].data_ptr() for i in range(k)])
+        caps = (ctypes.c_int64 * k)(*([cap] * k))
+        nrep = (ctypes.c_int64 * k)()
+        rc = lib.gss_check_passes_host(eng.h, k, sp, wl.n_vars, wl.n_words, ctypes.c_void_p(start_h.data_ptr()),
+                                       ctypes.c_void_p(sow_h.data_ptr()), op, caps, nrep)
         g._check(rc)
+        assert all(nrep[i] == n_reports for i in range(k)), list(nrep)
 
-    for _ in range(max(1, args.warmup)):
-        e2e_step()
+    e2e_run(max(2, args.warmup))
     barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(args.e2e_steps):
-        e2e_step()
+    e2e_run(args.e2e_steps)
     torch.cuda.synchronize()
     e2e_s = max_over_ranks((time.perf_counter() - t0) / args.e2e_steps, world, "cuda")
-    assert nrep.value == n_reports
     h2d = wl.state.nbytes + wl.start.nbytes + wl.solver_of_word.nbytes
     d2h = n_reports * 16 + 16 * 4
 
@@ -336,7 +353,9 @@ def run_gpu(args):
         B = algorithmic_bytes(wl, n_reports)
         achieved = B / kern_avg_s / 1e9
         roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                    "frac": achieved / peak, "traffic": load_traffic(),
+                    "frac": achieved / peak,
+                    "traffic": load_traffic() if (args.workload == "scale" and args.clauses == 4_000_000
+                                                  and args.kind is None) else None,
                     "algorithmic_bytes_per_launch": B, "kernel_ms": kern_avg_s * 1e3,
                     "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                     else "fallback"}
@@ -363,6 +382,8 @@ def run_gpu(args):
 
 def main():
     args = parse()
+    if args.clauses is None:
+        args.clauses = 100_000 if args.workload == "small" else 4_000_000
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -81,6 +81,7 @@ def load():
     _sig(lib, "gss_check_wait", c_int, vp, vp)
     _sig(lib, "gss_check_copy_reports", c_int, vp, vp, c_i64, vp)
     _sig(lib, "gss_check_pass_host", c_int, vp, vp, c_i64, c_int, vp, vp, vp, c_i64, vp)
+    _sig(lib, "gss_check_passes_host", c_int, vp, c_int, vp, c_i64, c_int, vp, vp, vp, vp, vp)
     _lib = lib
     return lib
 
@@ -199,6 +200,30 @@ class Engine:
                 continue
             _check(rc)
             return out[:n.value]
+
+
+def passes_host(engine, states, start, solver_of_word=None, caps=None):
+    """Pipelined passes through host buffers (gss_check_passes_host); returns
+    one report array per state."""
+    lib = engine.lib
+    n = len(states)
+    states = [np.ascontiguousarray(s, dtype=np.uint32) for s in states]
+    start = np.ascontiguousarray(start, dtype=np.uint32)
+    sow = None if solver_of_word is None else np.ascontiguousarray(solver_of_word, dtype=np.int32)
+    caps = caps or [1 << 20] * n
+    while True:
+        outs = [np.zeros(max(int(c), 1), dtype=REPORT_DTYPE) for c in caps]
+        sp = (ctypes.c_void_p * n)(*[s.ctypes.data for s in states])
+        op = (ctypes.c_void_p * n)(*[o.ctypes.data for o in outs])
+        cp = np.ascontiguousarray(caps, dtype=np.int64)
+        nr = np.zeros(n, dtype=np.int64)
+        rc = lib.gss_check_passes_host(engine.h, n, sp, states[0].shape[0], states[0].shape[1], _ptr(start), _ptr(sow),
+                                       op, _ptr(cp), _ptr(nr))
+        if rc == GSS_ERR_OVERFLOW:
+            caps = [max(int(c), int(x)) + 1024 for c, x in zip(caps, nr)]
+            continue
+        _check(rc)
+        return [o[:k] for o, k in zip(outs, nr)]
 
 
 def sort_reports(rep):

@@ -130,6 +130,13 @@ struct gss_engine {
     PinnedBuf h_counts;
     bool pass_pending = false;
 
+    // pipelined passes through host buffers (gss_check_passes_host): second
+    // state and report buffers, copy streams and events
+    DevBuf state2, state_raw2, reports2, counts2;
+    PinnedBuf h_counts2;
+    cudaStream_t h2d = nullptr, d2h = nullptr;
+    cudaEvent_t ev_h2d[2] = {nullptr, nullptr}, ev_kernel[2] = {nullptr, nullptr}, ev_d2h[2] = {nullptr, nullptr};
+
     // optional CUDA-event timing of each check kernel (on the launch stream)
     bool timing = false;
     std::vector<cudaEvent_t> ev_pool;
@@ -201,6 +208,13 @@ int gss_engine_destroy(gss_engine *eng) {
     cudaSetDevice(eng->device);
     if (eng->stream) cudaStreamSynchronize(eng->stream);
     if (eng->own_stream) cudaStreamDestroy(eng->own_stream);
+    if (eng->h2d) cudaStreamDestroy(eng->h2d);
+    if (eng->d2h) cudaStreamDestroy(eng->d2h);
+    for (int b = 0; b < 2; b++) {
+        if (eng->ev_h2d[b]) cudaEventDestroy(eng->ev_h2d[b]);
+        if (eng->ev_kernel[b]) cudaEventDestroy(eng->ev_kernel[b]);
+        if (eng->ev_d2h[b]) cudaEventDestroy(eng->ev_d2h[b]);
+    }
     for (auto &p : eng->ev_pending) {
         cudaEventDestroy(p.first);
         cudaEventDestroy(p.second);
@@ -448,8 +462,29 @@ int gss_check_set_capacity(gss_engine *eng, int64_t records) {
     return GSS_OK;
 }
 
+namespace {
+
+// Launches one check pass of the engine's database against `state` (laid out
+// as the engine's current state), into `reports`/`counts`, then copies the
+// counts and the error flag into `h_counts` (pinned), all on the engine's
+// stream.
+int launch_pass_into(gss_engine *eng, const void *state, DevBuf &reports, DevBuf &counts, PinnedBuf &h_counts);
+
+}  // namespace
+
 int gss_check_launch(gss_engine *eng) {
     if (!eng) return set_error(GSS_ERR_INVALID, "engine is NULL");
+    GSS_TRY(ensure_device(eng));
+    GSS_TRY(ensure_queues(eng));
+    GSS_TRY(launch_pass_into(eng, eng->state.ptr, eng->reports, eng->counts, eng->h_counts));
+    eng->launches++;
+    eng->pass_pending = true;
+    return GSS_OK;
+}
+
+namespace {
+
+int launch_pass_into(gss_engine *eng, const void *state, DevBuf &reports, DevBuf &counts, PinnedBuf &h_counts) {
     if (eng->n_clauses > 0 && eng->max_var >= eng->n_vars)
         return set_error(GSS_ERR_INVALID, "database uses variable %lld but the state has %lld variables",
                          (long long) eng->max_var, (long long) eng->n_vars);
@@ -459,14 +494,12 @@ int gss_check_launch(gss_engine *eng) {
                          "changing the variant");
     if (eng->state_kind == GSS_KERNEL_DIRECT && !valid_variant(eng->state_lpc, eng->state_g) && eng->n_words > 0)
         return set_error(GSS_ERR_STATE, "no direct kernel variant for %d lanes per clause", eng->state_lpc);
-    GSS_TRY(ensure_device(eng));
-    GSS_TRY(ensure_queues(eng));
     CheckArgs a;
     a.lits = (const int32_t *) eng->lits.ptr;
     a.offsets = (const int64_t *) eng->offsets.ptr;
     a.orig = (const uint32_t *) eng->orig.ptr;
     a.n_clauses = (uint32_t) eng->n_clauses;
-    a.state = (const uint2 *) eng->state.ptr;
+    a.state = (const uint2 *) state;
     a.n_vars = (uint32_t) eng->n_vars;
     a.n_blocks = (uint32_t) eng->n_blocks;
     a.lpc = eng->state_lpc;
@@ -479,8 +512,8 @@ int gss_check_launch(gss_engine *eng) {
     a.err = (uint32_t *) eng->err.ptr;
     a.start = (const uint32_t *) eng->start.ptr;
     a.solver_of_word = (const int32_t *) eng->solver_of_word.ptr;
-    a.out = (gss_report *) eng->reports.ptr;
-    a.counts = (uint32_t *) eng->counts.ptr;
+    a.out = (gss_report *) reports.ptr;
+    a.counts = (uint32_t *) counts.ptr;
     a.n_parts = eng->n_parts;
     a.cap_per_part = eng->cap_per_part;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -513,14 +546,15 @@ int gss_check_launch(gss_engine *eng) {
         GSS_CUDA_TRY(cudaEventRecord(ev1, eng->stream));
         eng->ev_pending.emplace_back(ev0, ev1);
     }
-    GSS_CUDA_TRY(cudaMemcpyAsync(eng->h_counts.ptr, eng->counts.ptr, sizeof(uint32_t) * eng->n_parts,
+    GSS_CUDA_TRY(cudaMemcpyAsync(h_counts.ptr, counts.ptr, sizeof(uint32_t) * eng->n_parts, cudaMemcpyDeviceToHost,
+                                 eng->stream));
+    GSS_CUDA_TRY(cudaMemcpyAsync((uint32_t *) h_counts.ptr + eng->n_parts, a.err, sizeof(uint32_t),
                                  cudaMemcpyDeviceToHost, eng->stream));
-    GSS_CUDA_TRY(cudaMemcpyAsync((uint32_t *) eng->h_counts.ptr + eng->n_parts, a.err, sizeof(uint32_t),
-                                 cudaMemcpyDeviceToHost, eng->stream));
-    eng->launches++;
-    eng->pass_pending = true;
     return GSS_OK;
 }
+
+}  // namespace
+
 
 int gss_check_wait(gss_engine *eng, int64_t *n_reports) {
     if (!eng) return set_error(GSS_ERR_INVALID, "engine is NULL");
@@ -578,6 +612,132 @@ int gss_check_pass_host(gss_engine *eng, const uint32_t *state, int64_t n_vars, 
         return gss_check_copy_reports(eng, out, cap, n_reports);
     }
     return set_error(GSS_ERR_OVERFLOW, "report queues kept overflowing");
+}
+
+int gss_check_passes_host(gss_engine *eng, int n_passes, const uint32_t *const *states, int64_t n_vars,
+                          int n_words, const uint32_t *start, const int32_t *solver_of_word, gss_report *const *outs,
+                          const int64_t *caps, int64_t *n_reports) {
+    // Passes i = 0..n-1 over three streams: the state of pass i+1 goes
+    // host->device (h2d stream) and the reports of pass i-1 come back (d2h
+    // stream) while pass i runs (engine stream). Double buffers: state b and
+    // report set b belong to passes b, b+2, b+4...
+    if (!eng || n_passes < 0 || (n_passes > 0 && (!states || !outs || !caps || !n_reports)))
+        return set_error(GSS_ERR_INVALID, "bad arguments to gss_check_passes_host");
+    if (n_passes == 0) return GSS_OK;
+    GSS_TRY(ensure_device(eng));
+    // layout, start and solver words from the first pass (copies its state too)
+    GSS_TRY(gss_state_set(eng, states[0], n_vars, n_words, start, solver_of_word, 0));
+    GSS_TRY(ensure_queues(eng));
+    const bool direct = eng->n_blocks == 1 && eng->n_words == eng->state_bw;
+    const size_t sbytes = (size_t) n_vars * n_words * 2 * sizeof(uint32_t);
+    const size_t bbytes = (size_t) eng->n_blocks * n_vars * eng->state_bw * sizeof(uint2);
+    if (!eng->h2d) GSS_CUDA_TRY(cudaStreamCreateWithFlags(&eng->h2d, cudaStreamNonBlocking));
+    if (!eng->d2h) GSS_CUDA_TRY(cudaStreamCreateWithFlags(&eng->d2h, cudaStreamNonBlocking));
+    for (int b = 0; b < 2; b++) {
+        if (!eng->ev_h2d[b]) GSS_CUDA_TRY(cudaEventCreateWithFlags(&eng->ev_h2d[b], cudaEventDisableTiming));
+        if (!eng->ev_kernel[b]) GSS_CUDA_TRY(cudaEventCreateWithFlags(&eng->ev_kernel[b], cudaEventDisableTiming));
+        if (!eng->ev_d2h[b]) GSS_CUDA_TRY(cudaEventCreateWithFlags(&eng->ev_d2h[b], cudaEventDisableTiming));
+    }
+    GSS_TRY(eng->state2.reserve(std::max<size_t>(bbytes, 8)));
+    if (!direct) {
+        GSS_TRY(eng->state_raw.reserve(std::max<size_t>(sbytes, 8)));
+        GSS_TRY(eng->state_raw2.reserve(std::max<size_t>(sbytes, 8)));
+    }
+    GSS_TRY(eng->reports2.reserve((size_t) eng->cap_per_part * eng->n_parts * sizeof(gss_report)));
+    GSS_TRY(eng->counts2.reserve(sizeof(uint32_t) * eng->n_parts));
+    GSS_TRY(eng->h_counts2.reserve(sizeof(uint32_t) * (eng->n_parts + 1)));
+    DevBuf *state_buf[2] = {&eng->state, &eng->state2};
+    DevBuf *raw_buf[2] = {&eng->state_raw, &eng->state_raw2};
+    DevBuf *rep_buf[2] = {&eng->reports, &eng->reports2};
+    DevBuf *cnt_buf[2] = {&eng->counts, &eng->counts2};
+    PinnedBuf *hcnt_buf[2] = {&eng->h_counts, &eng->h_counts2};
+    GSS_CUDA_TRY(cudaStreamSynchronize(eng->stream));  // pass 0's state is in buffer 0
+
+    int launched = 0;
+    // copies the reports of pass j back (the host waits for its kernel)
+    auto finish = [&](int j) -> int {
+        const int b = j & 1;
+        GSS_CUDA_TRY(cudaEventSynchronize(eng->ev_kernel[b]));
+        const uint32_t *hc = (const uint32_t *) hcnt_buf[b]->ptr;
+        if (hc[eng->n_parts] != 0)
+            return set_error(GSS_ERR_CUDA, "a bounded wait in the check kernel gave up (pass %d)", j);
+        int64_t total = 0;
+        bool overflow = false;
+        for (uint32_t p = 0; p < eng->n_parts; p++) {
+            total += hc[p];
+            overflow |= hc[p] > eng->cap_per_part;
+        }
+        if (overflow) {
+            // Rare after the first passes: grow both report sets and check this
+            // pass again from its state buffer (not reused before pass j+2).
+            // Pass j+1, already launched into the other set, runs again too:
+            // growing the sets drops what it wrote.
+            GSS_CUDA_TRY(cudaDeviceSynchronize());
+            eng->requested_cap = std::max<int64_t>(eng->requested_cap, total * 2 + eng->n_parts * 1024);
+            GSS_TRY(ensure_queues(eng));
+            GSS_TRY(eng->reports2.reserve((size_t) eng->cap_per_part * eng->n_parts * sizeof(gss_report)));
+            GSS_TRY(launch_pass_into(eng, state_buf[b]->ptr, *rep_buf[b], *cnt_buf[b], *hcnt_buf[b]));
+            eng->launches++;
+            GSS_CUDA_TRY(cudaEventRecord(eng->ev_kernel[b], eng->stream));
+            if (j + 1 < launched) {
+                const int nb = b ^ 1;
+                GSS_TRY(launch_pass_into(eng, state_buf[nb]->ptr, *rep_buf[nb], *cnt_buf[nb], *hcnt_buf[nb]));
+                eng->launches++;
+                GSS_CUDA_TRY(cudaEventRecord(eng->ev_kernel[nb], eng->stream));
+            }
+            GSS_CUDA_TRY(cudaEventSynchronize(eng->ev_kernel[b]));
+            total = 0;
+            for (uint32_t p = 0; p < eng->n_parts; p++) total += hc[p];
+        }
+        n_reports[j] = total;
+        if (total > caps[j])
+            return set_error(GSS_ERR_OVERFLOW, "output %d holds %lld records, pass has %lld", j, (long long) caps[j],
+                             (long long) total);
+        int64_t pos = 0;
+        for (uint32_t p = 0; p < eng->n_parts; p++) {
+            if (!hc[p]) continue;
+            GSS_CUDA_TRY(cudaMemcpyAsync(outs[j] + pos, (gss_report *) rep_buf[b]->ptr + (size_t) p * eng->cap_per_part,
+                                         (size_t) hc[p] * sizeof(gss_report), cudaMemcpyDeviceToHost, eng->d2h));
+            pos += hc[p];
+        }
+        GSS_CUDA_TRY(cudaEventRecord(eng->ev_d2h[b], eng->d2h));
+        return GSS_OK;
+    };
+
+    auto pipeline = [&]() -> int {
+    for (int i = 0; i < n_passes; i++) {
+        const int b = i & 1;
+        if (i > 0) {
+            // state i -> buffer b, once pass i-2 (the last reader of b) is done
+            if (i >= 2) GSS_CUDA_TRY(cudaStreamWaitEvent(eng->h2d, eng->ev_kernel[b], 0));
+            void *dst = direct ? state_buf[b]->ptr : raw_buf[b]->ptr;
+            if (!states[i]) return set_error(GSS_ERR_INVALID, "state %d is NULL", i);
+            GSS_CUDA_TRY(cudaMemcpyAsync(dst, states[i], sbytes, cudaMemcpyHostToDevice, eng->h2d));
+            GSS_CUDA_TRY(cudaEventRecord(eng->ev_h2d[b], eng->h2d));
+            GSS_CUDA_TRY(cudaStreamWaitEvent(eng->stream, eng->ev_h2d[b], 0));
+            if (!direct)
+                GSS_TRY(launch_relayout((const uint2 *) raw_buf[b]->ptr, (uint2 *) state_buf[b]->ptr, (uint32_t) n_vars,
+                                        (uint32_t) n_words, (uint32_t) eng->state_bw, (uint32_t) eng->n_blocks,
+                                        eng->stream, eng->sm_count));
+        }
+        // report set b is free once pass i-2's reports are back
+        if (i >= 2) GSS_CUDA_TRY(cudaStreamWaitEvent(eng->stream, eng->ev_d2h[b], 0));
+        GSS_TRY(launch_pass_into(eng, state_buf[b]->ptr, *rep_buf[b], *cnt_buf[b], *hcnt_buf[b]));
+        eng->launches++;
+        launched = i + 1;
+        GSS_CUDA_TRY(cudaEventRecord(eng->ev_kernel[b], eng->stream));
+        if (i > 0) GSS_TRY(finish(i - 1));
+    }
+    GSS_TRY(finish(n_passes - 1));
+    GSS_CUDA_TRY(cudaStreamSynchronize(eng->d2h));
+    return GSS_OK;
+    };
+    const int rc = pipeline();
+    // on an early error, let everything already queued finish before the
+    // buffers can be reused
+    if (rc != GSS_OK) cudaDeviceSynchronize();
+    eng->pass_pending = false;
+    return rc;
 }
 
 }  // extern "C"

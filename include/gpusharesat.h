@@ -149,6 +149,15 @@ int gss_check_copy_reports(gss_engine *eng, gss_report *out, int64_t cap, int64_
 int gss_check_pass_host(gss_engine *eng, const uint32_t *state, int64_t n_vars, int n_words,
                         const uint32_t *start, const int32_t *solver_of_word,
                         gss_report *out, int64_t cap, int64_t *n_reports);
+/* n_passes whole passes through host buffers, pipelined: while pass i is
+ * checked, the state of pass i+1 is copied in and the reports of pass i-1
+ * copied out (pinned host buffers make the copies overlap). states[i] (host)
+ * holds pass i's bit planes, all with the same n_vars, n_words, start and
+ * solver_of_word; outs[i] (host, caps[i] records) receives its reports and
+ * n_reports[i] their count. Synchronous: returns when every output is filled. */
+int gss_check_passes_host(gss_engine *eng, int n_passes, const uint32_t *const *states, int64_t n_vars,
+                          int n_words, const uint32_t *start, const int32_t *solver_of_word,
+                          gss_report *const *outs, const int64_t *caps, int64_t *n_reports);
 
 /* ---- allocation-free check pass ----
  * No counterpart in the reference. For callers that cannot allocate device
