@@ -29,6 +29,7 @@ KERNEL_WIDE2 = 3
 VARIANT_L2_HINT = 1
 VARIANT_OCCUPANCY = 2
 VARIANT_PIPELINED = 4
+VARIANT_PERSISTENT = 8
 
 REPORT_DTYPE = np.dtype([("clause", "<u4"), ("word", "<u4"), ("mask", "<u4"), ("solver", "<u4")])
 
@@ -69,14 +70,21 @@ def load():
     _sig(lib, "gss_engine_set_stream", c_int, vp, vp)
     _sig(lib, "gss_engine_launch_count", c_i64, vp)
     _sig(lib, "gss_engine_set_timing", c_int, vp, c_int)
+    _sig(lib, "gss_engine_set_graph", c_int, vp, c_int)
+    _sig(lib, "gss_engine_graph_captures", c_i64, vp)
     _sig(lib, "gss_engine_kernel_time", c_int, vp, vp, vp)
     _sig(lib, "gss_engine_set_variant", c_int, vp, c_int, c_int, c_int, c_int)
     _sig(lib, "gss_db_set", c_int, vp, vp, vp, c_i64)
     _sig(lib, "gss_db_clause_count", c_i64, vp)
+    _sig(lib, "gss_db_append", c_int, vp, vp, vp, c_i64, vp)
+    _sig(lib, "gss_db_delete", c_int, vp, vp, c_i64)
+    _sig(lib, "gss_db_compact", c_int, vp)
+    _sig(lib, "gss_db_live_count", c_i64, vp)
     _sig(lib, "gss_db_literal_count", c_i64, vp)
     _sig(lib, "gss_db_max_var", c_i64, vp)
     _sig(lib, "gss_state_set", c_int, vp, vp, c_i64, c_int, vp, vp, c_int)
     _sig(lib, "gss_check_set_capacity", c_int, vp, c_i64)
+    _sig(lib, "gss_state_set_start", c_int, vp, vp, c_int)
     _sig(lib, "gss_check_launch", c_int, vp)
     _sig(lib, "gss_check_wait", c_int, vp, vp)
     _sig(lib, "gss_check_copy_reports", c_int, vp, vp, c_i64, vp)
@@ -128,6 +136,13 @@ class Engine:
     def launch_count(self):
         return int(self.lib.gss_engine_launch_count(self.h))
 
+    def set_graph(self, on=True):
+        _check(self.lib.gss_engine_set_graph(self.h, 1 if on else 0))
+
+    @property
+    def graph_captures(self):
+        return int(self.lib.gss_engine_graph_captures(self.h))
+
     def set_timing(self, on=True):
         _check(self.lib.gss_engine_set_timing(self.h, 1 if on else 0))
 
@@ -147,6 +162,27 @@ class Engine:
         offsets = np.ascontiguousarray(offsets, dtype=np.int64)
         _check(self.lib.gss_db_set(self.h, _ptr(lits), _ptr(offsets), offsets.shape[0] - 1))
 
+    def append_db(self, lits, offsets, ids=None):
+        lits = np.ascontiguousarray(lits, dtype=np.int32)
+        offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+        ids = None if ids is None else np.ascontiguousarray(ids, dtype=np.uint32)
+        _check(self.lib.gss_db_append(self.h, _ptr(lits), _ptr(offsets), offsets.shape[0] - 1, _ptr(ids)))
+
+    def delete(self, ids):
+        ids = np.ascontiguousarray(ids, dtype=np.uint32)
+        _check(self.lib.gss_db_delete(self.h, _ptr(ids), ids.shape[0]))
+
+    def compact(self):
+        _check(self.lib.gss_db_compact(self.h))
+
+    @property
+    def live_count(self):
+        return int(self.lib.gss_db_live_count(self.h))
+
+    @property
+    def clause_count(self):
+        return int(self.lib.gss_db_clause_count(self.h))
+
     def set_state(self, state, start, solver_of_word=None):
         state = np.ascontiguousarray(state, dtype=np.uint32)
         start = np.ascontiguousarray(start, dtype=np.uint32)
@@ -157,6 +193,10 @@ class Engine:
     def set_state_device(self, state_ptr, n_vars, n_words, start_ptr, sow_ptr=None):
         _check(self.lib.gss_state_set(self.h, _vp(state_ptr), n_vars, n_words, _vp(start_ptr),
                                       _vp(sow_ptr) if sow_ptr else None, 1))
+
+    def set_start(self, start):
+        start = np.ascontiguousarray(start, dtype=np.uint32)
+        _check(self.lib.gss_state_set_start(self.h, _ptr(start), start.shape[0]))
 
     def set_capacity(self, records):
         _check(self.lib.gss_check_set_capacity(self.h, int(records)))

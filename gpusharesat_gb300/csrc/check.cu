@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(kWarps * 32) check_kernel(CheckArgs a) {
         const uint32_t blk = (uint32_t) (task / n_groups);
         const uint32_t g = (uint32_t) (task - (uint64_t) blk * n_groups);
         const uint32_t c = g * CPW + grp;
-        const bool valid = c < a.n_clauses;
+        const bool valid = c < a.n_clauses && clause_live(a, c);
         const uint32_t w = blk * LPC + sub;
         uint32_t all_false = valid ? __ldg(a.start + w) : 0u;  // start is padded to n_blocks*LPC
         uint32_t one_undef = 0;
@@ -263,7 +263,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) check_wide_kernel(CheckArgs
         const uint32_t blk = (uint32_t) (task / n_groups);
         const uint32_t g = (uint32_t) (task - (uint64_t) blk * n_groups);
         const uint32_t c = g * CPW + grp;
-        const bool valid = c < a.n_clauses;
+        const bool valid = c < a.n_clauses && clause_live(a, c);
         const uint32_t w0 = blk * BW + sub * WPL;
         uint32_t af[WPL], ou[WPL];
 #pragma unroll
@@ -388,7 +388,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) check_wide_pf_kernel(CheckA
     for (; task < n_tasks; task += stride) {
         const uint32_t blk = (uint32_t) (task / n_groups);
         const uint32_t c = clause_of(task);
-        const bool valid = c < a.n_clauses;
+        const bool valid = c < a.n_clauses && clause_live(a, c);
         const uint32_t w0 = blk * BW + sub * WPL;
         uint32_t af[WPL], ou[WPL];
 #pragma unroll
@@ -401,7 +401,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) check_wide_pf_kernel(CheckA
         // start the next task's offsets now
         const uint64_t nt = task + stride;
         const uint32_t nc = nt < n_tasks ? clause_of(nt) : 0xFFFFFFFFu;
-        const bool nvalid = nt < n_tasks && nc < a.n_clauses;
+        const bool nvalid = nt < n_tasks && nc < a.n_clauses && clause_live(a, nc);
         nx_pos = nvalid ? (uint32_t) __ldg(a.offsets + nc) : 0u;
         nx_end = nvalid ? (uint32_t) __ldg(a.offsets + nc + 1) : 0u;
         bool next_chunk_due = true;
@@ -475,6 +475,135 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) check_wide_pf_kernel(CheckA
         }
     }
     if (nstaged) flush_stage(stage, nstaged, out, counter, a.cap_per_part, lane);
+}
+
+// Persistent wide variant: as check_wide_kernel, with (1) its arguments read
+// from device memory, so a captured CUDA graph can run it pass after pass
+// while the database and the assignment state change, and (2) tasks taken in
+// chunks from a device work counter (zeroed before the launch) instead of a
+// fixed stride, so clauses of very different lengths balance across warps.
+constexpr uint32_t kTaskChunk = 4;
+
+template <int WPL, int LPC, int G>
+__global__ void __launch_bounds__(kWarps * 32, 1) check_wide_persist_kernel(const CheckArgs *__restrict__ pa,
+                                                                             uint32_t *__restrict__ work) {
+    constexpr int CPW = 32 / LPC;
+    constexpr int BW = WPL * LPC;
+    __shared__ CheckArgs sa;
+    __shared__ gss_report stage_all[kWarps][kStage];
+    if (threadIdx.x == 0) sa = *pa;
+    __syncthreads();
+    const CheckArgs &a = sa;
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int sub = lane % LPC;
+    const int grp = lane / LPC;
+    const int gbase = grp * LPC;
+    gss_report *stage = stage_all[wib];
+    const uint32_t part = blockIdx.x % a.n_parts;
+    gss_report *out = a.out + (size_t) part * a.cap_per_part;
+    uint32_t *counter = a.counts + part;
+    uint32_t nstaged = 0;
+
+    const uint32_t n_groups = (a.n_clauses + CPW - 1) / CPW;
+    const uint64_t n_tasks = (uint64_t) n_groups * a.n_blocks;
+    while (true) {
+        uint32_t first = 0;
+        if (lane == 0) first = atomicAdd(work, kTaskChunk);
+        first = __shfl_sync(kFull, first, 0);
+        if ((uint64_t) first >= n_tasks) break;
+        const uint64_t last = min((uint64_t) first + kTaskChunk, n_tasks);
+        for (uint64_t task = first; task < last; task++) {
+            const uint32_t blk = (uint32_t) (task / n_groups);
+            const uint32_t g = (uint32_t) (task - (uint64_t) blk * n_groups);
+            const uint32_t c = g * CPW + grp;
+            const bool valid = c < a.n_clauses && clause_live(a, c);
+            const uint32_t w0 = blk * BW + sub * WPL;
+            uint32_t af[WPL], ou[WPL];
+#pragma unroll
+            for (int j = 0; j < WPL; j++) {
+                af[j] = valid ? __ldg(a.start + w0 + j) : 0u;
+                ou[j] = 0u;
+            }
+            uint32_t pos = 0, end = 0;
+            if (valid) {
+                pos = (uint32_t) __ldg(a.offsets + c);
+                end = (uint32_t) __ldg(a.offsets + c + 1);
+            }
+            const uint2 *rows = a.state + (size_t) blk * a.n_vars * BW + sub * WPL;
+            while (true) {
+                bool alive = false;
+#pragma unroll
+                for (int j = 0; j < WPL; j++) alive |= (af[j] | ou[j]) != 0u;
+                if (!__any_sync(kFull, alive && pos < end)) break;
+                const int32_t chunk = (pos + sub < end) ? __ldg(a.lits + pos + sub) : 0;
+                const int navail = (int) min((uint32_t) LPC, end > pos ? end - pos : 0u);
+#pragma unroll 1
+                for (int k0 = 0; k0 < LPC; k0 += G) {
+                    alive = false;
+#pragma unroll
+                    for (int j = 0; j < WPL; j++) alive |= (af[j] | ou[j]) != 0u;
+                    if (!__any_sync(kFull, alive && k0 < navail)) break;
+                    uint32_t lit[G];
+                    Row<WPL> st[G];
+#pragma unroll
+                    for (int i = 0; i < G; i++) lit[i] = (uint32_t) __shfl_sync(kFull, chunk, gbase + k0 + i);
+#pragma unroll
+                    for (int i = 0; i < G; i++) {
+#pragma unroll
+                        for (int q = 0; q < 2 * WPL; q++) st[i].v[q] = 0u;
+                        if (alive && k0 + i < navail) ld_row<WPL>(rows + (size_t) (lit[i] >> 1) * BW, st[i]);
+                    }
+#pragma unroll
+                    for (int i = 0; i < G; i++) {
+                        if (k0 + i < navail) {
+                            const bool neg = (lit[i] & 1u) != 0u;
+#pragma unroll
+                            for (int j = 0; j < WPL; j++) {
+                                const uint32_t d = st[i].v[2 * j], t = st[i].v[2 * j + 1];
+                                const uint32_t f = (neg ? t : ~t) & d;
+                                ou[j] = (af[j] & ~d) | (ou[j] & f);
+                                af[j] &= f;
+                            }
+                        }
+                    }
+                }
+                pos += LPC;
+            }
+#pragma unroll
+            for (int j = 0; j < WPL; j++) {
+                const uint32_t rep = af[j] | ou[j];
+                const unsigned bal = __ballot_sync(kFull, rep != 0u);
+                if (bal) {
+                    if (nstaged + 32 > (uint32_t) kStage) {
+                        flush_stage(stage, nstaged, out, counter, a.cap_per_part, lane);
+                        nstaged = 0;
+                    }
+                    if (rep) {
+                        gss_report r;
+                        r.clause = __ldg(a.orig + c);
+                        r.word = w0 + j;
+                        r.mask = rep;
+                        r.solver = (uint32_t) __ldg(a.solver_of_word + w0 + j);
+                        stage[nstaged + __popc(bal & lanemask_lt())] = r;
+                    }
+                    nstaged += __popc(bal);
+                }
+            }
+        }
+    }
+    if (nstaged) flush_stage(stage, nstaged, out, counter, a.cap_per_part, lane);
+}
+
+template <int WPL, int LPC, int G>
+int launch_wide_persist_variant(const CheckArgs *d_args, uint32_t *work, cudaStream_t stream, int sm_count) {
+    int per_sm = 0;
+    GSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, check_wide_persist_kernel<WPL, LPC, G>,
+                                                               kWarps * 32, 0));
+    if (per_sm < 1) per_sm = 1;
+    check_wide_persist_kernel<WPL, LPC, G><<<(unsigned) (sm_count * per_sm), kWarps * 32, 0, stream>>>(d_args, work);
+    GSS_CUDA_TRY(cudaGetLastError());
+    return GSS_OK;
 }
 
 template <int WPL, int LPC, int G, int MINB>
@@ -569,6 +698,25 @@ int launch_check_wide_pf(const CheckArgs &a, int wpl, int occ, cudaStream_t stre
 #undef GSS_PV
     return set_error(GSS_ERR_INVALID, "no pipelined wide kernel variant for %d words per lane, %d lanes, depth %d",
                      wpl, a.lpc, a.g);
+}
+
+int launch_check_wide_persist(const CheckArgs *d_args, int wpl, int lpc, int g, uint32_t *work, cudaStream_t stream,
+                              int sm_count) {
+#define GSS_QV(W, L, GG) \
+    if (wpl == W && lpc == L && g == GG) return launch_wide_persist_variant<W, L, GG>(d_args, work, stream, sm_count);
+    GSS_QV(4, 8, 1) GSS_QV(4, 8, 2) GSS_QV(4, 8, 4)
+    GSS_QV(4, 4, 2) GSS_QV(4, 2, 2)
+    GSS_QV(2, 16, 2) GSS_QV(2, 8, 2)
+#undef GSS_QV
+    return set_error(GSS_ERR_INVALID, "no persistent wide kernel variant for %d words per lane, %d lanes, depth %d",
+                     wpl, lpc, g);
+}
+
+bool valid_wide_persist_variant(int wpl, int lpc, int g) {
+    if (wpl == 4 && lpc == 8) return g == 1 || g == 2 || g == 4;
+    if (wpl == 4 && (lpc == 4 || lpc == 2)) return g == 2;
+    if (wpl == 2 && (lpc == 16 || lpc == 8)) return g == 2;
+    return false;
 }
 
 bool valid_wide_pf_variant(int wpl, int lpc, int g) {

@@ -83,7 +83,13 @@ struct CheckArgs {
     const uint32_t *tile_lit;     // device, n_tiles + 1: first literal of each tile
     uint32_t n_tiles;
     uint32_t *err;                // device flag, set to nonzero when a bounded wait gives up
+    const uint32_t *alive;        // device, 1 bit per clause (NULL: every clause is live)
 };
+
+// Whether clause c of the database takes part in the pass.
+__device__ __forceinline__ bool clause_live(const CheckArgs &a, uint32_t c) {
+    return a.alive == nullptr || ((__ldg(a.alive + (c >> 5)) >> (c & 31)) & 1u);
+}
 
 // Launches the check kernel on `stream` (the counters must already be zero).
 // Returns a GSS status.
@@ -94,6 +100,11 @@ int launch_check_wide(const CheckArgs &a, int wpl, int occ, cudaStream_t stream,
 // Pipelined wide kernel (occ: 4 blocks per SM register cap).
 int launch_check_wide_pf(const CheckArgs &a, int wpl, int occ, cudaStream_t stream, int sm_count);
 bool valid_wide_pf_variant(int wpl, int lpc, int g);
+// Persistent wide kernel: arguments read from device memory (d_args), tasks
+// from the device counter `work` (zero it before each launch).
+int launch_check_wide_persist(const CheckArgs *d_args, int wpl, int lpc, int g, uint32_t *work, cudaStream_t stream,
+                              int sm_count);
+bool valid_wide_persist_variant(int wpl, int lpc, int g);
 bool valid_wide_variant(int wpl, int lpc, int g, int occ);
 bool valid_tiled_variant(int lpc, int k);
 

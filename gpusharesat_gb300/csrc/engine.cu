@@ -104,6 +104,18 @@ struct gss_engine {
     // tiles of the tiled kernel (first clause / first literal of each tile)
     DevBuf tile_clause, tile_lit;
     uint32_t n_tiles = 0;
+    bool tiles_stale = true;
+    // host mirror of the database, in device order, for appends, deletes and
+    // compaction; alive bits (1 per device clause) mark deleted clauses
+    std::vector<int32_t> h_lits;
+    std::vector<int64_t> h_off;
+    std::vector<uint32_t> h_ids;
+    std::vector<uint32_t> index_of;  // clause id -> device index (0xFFFFFFFF: none)
+    std::vector<uint32_t> h_alive;
+    DevBuf alive;
+    bool alive_dirty = false;
+    int64_t n_dead = 0;
+    uint32_t next_id = 0;
 
     // kernel variant: kind (GSS_KERNEL_*), lanes (words) per clause (0 = pick
     // from the word count), loads in flight / clause slots, cache hints
@@ -136,6 +148,16 @@ struct gss_engine {
     PinnedBuf h_counts2;
     cudaStream_t h2d = nullptr, d2h = nullptr;
     cudaEvent_t ev_h2d[2] = {nullptr, nullptr}, ev_kernel[2] = {nullptr, nullptr}, ev_d2h[2] = {nullptr, nullptr};
+
+    // persistent kernel: arguments in device memory, task counter; optional
+    // CUDA graph of a pass (memsets, kernel, count readback), recaptured when
+    // a buffer it names changes
+    DevBuf d_args, work;
+    bool use_graph = false;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    std::vector<uintptr_t> graph_key;
+    int64_t graph_captures = 0;
 
     // optional CUDA-event timing of each check kernel (on the launch stream)
     bool timing = false;
@@ -208,6 +230,8 @@ int gss_engine_destroy(gss_engine *eng) {
     cudaSetDevice(eng->device);
     if (eng->stream) cudaStreamSynchronize(eng->stream);
     if (eng->own_stream) cudaStreamDestroy(eng->own_stream);
+    if (eng->graph_exec) cudaGraphExecDestroy(eng->graph_exec);
+    if (eng->graph) cudaGraphDestroy(eng->graph);
     if (eng->h2d) cudaStreamDestroy(eng->h2d);
     if (eng->d2h) cudaStreamDestroy(eng->d2h);
     for (int b = 0; b < 2; b++) {
@@ -231,6 +255,14 @@ int gss_engine_set_stream(gss_engine *eng, void *stream) {
 }
 
 int64_t gss_engine_launch_count(const gss_engine *eng) { return eng ? eng->launches : -1; }
+
+int gss_engine_set_graph(gss_engine *eng, int on) {
+    if (!eng) return set_error(GSS_ERR_INVALID, "engine is NULL");
+    eng->use_graph = on != 0;
+    return GSS_OK;
+}
+
+int64_t gss_engine_graph_captures(const gss_engine *eng) { return eng ? eng->graph_captures : -1; }
 
 int gss_engine_set_timing(gss_engine *eng, int on) {
     if (!eng) return set_error(GSS_ERR_INVALID, "engine is NULL");
@@ -258,77 +290,219 @@ int gss_engine_kernel_time(gss_engine *eng, double *total_ms, int64_t *n_launche
     return GSS_OK;
 }
 
-int gss_db_set(gss_engine *eng, const int32_t *lits, const int64_t *offsets, int64_t n_clauses) {
-    if (!eng || !offsets || n_clauses < 0) return set_error(GSS_ERR_INVALID, "bad arguments to gss_db_set");
-    if (n_clauses > 0xFFFFFFF0LL) return set_error(GSS_ERR_INVALID, "too many clauses (%lld)", (long long) n_clauses);
-    if (offsets[0] != 0) return set_error(GSS_ERR_INVALID, "offsets[0] must be 0");
-    // Counting sort by length, stable: equal-length clauses keep their order,
-    // as in the reference's per-size buckets (Clauses.cu:47-51).
-    std::vector<int64_t> count(kMaxClauseLen + 2, 0);
-    for (int64_t c = 0; c < n_clauses; c++) {
-        int64_t len = offsets[c + 1] - offsets[c];
+namespace {
+
+// Checks a CSR batch (lengths 1..kMaxClauseLen, non-negative literals) and
+// returns its largest variable.
+int validate_batch(const int32_t *lits, const int64_t *offsets, int64_t n, int64_t &max_var) {
+    if (!offsets || n < 0) return set_error(GSS_ERR_INVALID, "bad clause batch");
+    if (n > 0 && offsets[0] != 0) return set_error(GSS_ERR_INVALID, "offsets[0] must be 0");
+    for (int64_t c = 0; c < n; c++) {
+        const int64_t len = offsets[c + 1] - offsets[c];
         if (len < 1 || len > kMaxClauseLen)
             return set_error(GSS_ERR_INVALID, "clause %lld has length %lld (allowed 1..%d)", (long long) c,
                              (long long) len, kMaxClauseLen);
-        count[len + 1]++;
     }
-    const int64_t n_lits = offsets[n_clauses];
+    const int64_t n_lits = n > 0 ? offsets[n] : 0;
     if (n_lits > 0 && !lits) return set_error(GSS_ERR_INVALID, "lits is NULL");
-    if (n_lits > 0x7FFFFF00LL) return set_error(GSS_ERR_INVALID, "too many literals (%lld)", (long long) n_lits);
-    int64_t max_var = -1;
+    max_var = -1;
     for (int64_t i = 0; i < n_lits; i++) {
         if (lits[i] < 0) return set_error(GSS_ERR_INVALID, "literal %lld is negative", (long long) i);
-        int64_t v = lits[i] >> 1;
-        if (v > max_var) max_var = v;
+        max_var = std::max<int64_t>(max_var, lits[i] >> 1);
     }
+    return GSS_OK;
+}
+
+// Stable counting sort of a batch by clause length, as the reference keeps
+// clauses in per-size buckets (Clauses.cu:47-51).
+void length_order(const int64_t *offsets, int64_t n, std::vector<uint32_t> &order) {
+    std::vector<int64_t> count(kMaxClauseLen + 2, 0);
+    for (int64_t c = 0; c < n; c++) count[offsets[c + 1] - offsets[c] + 1]++;
     for (int L = 1; L <= kMaxClauseLen + 1; L++) count[L] += count[L - 1];
-    std::vector<uint32_t> orig(n_clauses);
-    for (int64_t c = 0; c < n_clauses; c++) {
-        int64_t len = offsets[c + 1] - offsets[c];
-        orig[count[len]++] = (uint32_t) c;
-    }
-    std::vector<int64_t> soff(n_clauses + 1);
-    std::vector<int32_t> slits(n_lits);
-    soff[0] = 0;
-    for (int64_t i = 0; i < n_clauses; i++) {
-        const int64_t c = orig[i];
-        const int64_t len = offsets[c + 1] - offsets[c];
-        memcpy(&slits[soff[i]], lits + offsets[c], len * sizeof(int32_t));
-        soff[i + 1] = soff[i] + len;
-    }
-    // Tiles: greedy runs of sorted clauses with at most kTileLits literals; a
-    // longer clause is a tile on its own.
+    order.assign(n, 0);
+    for (int64_t c = 0; c < n; c++) order[count[offsets[c + 1] - offsets[c]]++] = (uint32_t) c;
+}
+
+// Tiles of the tiled kernel: greedy runs of clauses (in device order) with at
+// most kTileLits literals; a longer clause is a tile on its own.
+int upload_tiles(gss_engine *eng) {
+    const int64_t n = (int64_t) eng->h_off.size() - 1;
     std::vector<uint32_t> tclause, tlit;
-    for (int64_t i = 0; i < n_clauses;) {
+    for (int64_t i = 0; i < n;) {
         tclause.push_back((uint32_t) i);
-        tlit.push_back((uint32_t) soff[i]);
+        tlit.push_back((uint32_t) eng->h_off[i]);
         int64_t j = i + 1;
-        while (j < n_clauses && soff[j + 1] - soff[i] <= kTileLits) j++;
+        while (j < n && eng->h_off[j + 1] - eng->h_off[i] <= kTileLits) j++;
         i = j;
     }
-    tclause.push_back((uint32_t) n_clauses);
-    tlit.push_back((uint32_t) n_lits);
-    GSS_TRY(ensure_device(eng));
-    GSS_CUDA_TRY(cudaStreamSynchronize(eng->stream));
-    // 8 literals of zero padding: tile copies round their end up to 16 bytes
-    GSS_TRY(eng->lits.reserve((n_lits + 8) * sizeof(int32_t)));
-    GSS_CUDA_TRY(cudaMemset(eng->lits.ptr, 0, (n_lits + 8) * sizeof(int32_t)));
+    tclause.push_back((uint32_t) n);
+    tlit.push_back((uint32_t) eng->h_off[n]);
     GSS_TRY(eng->tile_clause.reserve(tclause.size() * sizeof(uint32_t)));
     GSS_TRY(eng->tile_lit.reserve(tlit.size() * sizeof(uint32_t)));
     GSS_CUDA_TRY(cudaMemcpy(eng->tile_clause.ptr, tclause.data(), tclause.size() * sizeof(uint32_t),
                             cudaMemcpyHostToDevice));
     GSS_CUDA_TRY(cudaMemcpy(eng->tile_lit.ptr, tlit.data(), tlit.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
     eng->n_tiles = (uint32_t) (tclause.size() - 1);
-    GSS_TRY(eng->offsets.reserve((n_clauses + 1) * sizeof(int64_t)));
-    GSS_TRY(eng->orig.reserve(std::max<int64_t>(n_clauses, 1) * sizeof(uint32_t)));
-    if (n_lits) GSS_CUDA_TRY(cudaMemcpy(eng->lits.ptr, slits.data(), n_lits * sizeof(int32_t), cudaMemcpyHostToDevice));
-    GSS_CUDA_TRY(cudaMemcpy(eng->offsets.ptr, soff.data(), (n_clauses + 1) * sizeof(int64_t), cudaMemcpyHostToDevice));
-    if (n_clauses) GSS_CUDA_TRY(cudaMemcpy(eng->orig.ptr, orig.data(), n_clauses * sizeof(uint32_t), cudaMemcpyHostToDevice));
-    eng->n_clauses = n_clauses;
+    eng->tiles_stale = false;
+    return GSS_OK;
+}
+
+// Copies the whole host mirror to the device (after a set or a compaction).
+int upload_all(gss_engine *eng) {
+    const int64_t n = (int64_t) eng->h_ids.size();
+    const int64_t n_lits = eng->h_off.back();
+    GSS_TRY(ensure_device(eng));
+    GSS_CUDA_TRY(cudaStreamSynchronize(eng->stream));
+    // 8 literals of zero padding: tile copies round their end up to 16 bytes
+    GSS_TRY(eng->lits.reserve((n_lits + 8) * sizeof(int32_t)));
+    GSS_CUDA_TRY(cudaMemset(eng->lits.ptr, 0, (n_lits + 8) * sizeof(int32_t)));
+    GSS_TRY(eng->offsets.reserve((n + 1) * sizeof(int64_t)));
+    GSS_TRY(eng->orig.reserve(std::max<int64_t>(n, 1) * sizeof(uint32_t)));
+    if (n_lits)
+        GSS_CUDA_TRY(cudaMemcpy(eng->lits.ptr, eng->h_lits.data(), n_lits * sizeof(int32_t), cudaMemcpyHostToDevice));
+    GSS_CUDA_TRY(cudaMemcpy(eng->offsets.ptr, eng->h_off.data(), (n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice));
+    if (n) GSS_CUDA_TRY(cudaMemcpy(eng->orig.ptr, eng->h_ids.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    eng->n_clauses = n;
     eng->n_lits = n_lits;
+    eng->n_dead = 0;
+    eng->h_alive.assign((n + 31) / 32, ~0u);
+    eng->alive_dirty = false;
+    eng->tiles_stale = true;
+    return GSS_OK;
+}
+
+// Adds a batch to the host mirror in length order; returns the first index.
+void mirror_append(gss_engine *eng, const int32_t *lits, const int64_t *offsets, int64_t n, const uint32_t *ids) {
+    std::vector<uint32_t> order;
+    length_order(offsets, n, order);
+    if (eng->h_off.empty()) eng->h_off.push_back(0);
+    for (int64_t k = 0; k < n; k++) {
+        const int64_t c = order[k];
+        const int64_t len = offsets[c + 1] - offsets[c];
+        eng->h_lits.insert(eng->h_lits.end(), lits + offsets[c], lits + offsets[c] + len);
+        eng->h_off.push_back(eng->h_off.back() + len);
+        const uint32_t id = ids ? ids[c] : (uint32_t) (eng->next_id + c);
+        if (id >= eng->index_of.size()) eng->index_of.resize((size_t) id + 1 + (id >> 3), 0xFFFFFFFFu);
+        eng->index_of[id] = (uint32_t) eng->h_ids.size();
+        eng->h_ids.push_back(id);
+    }
+    if (!ids) {
+        eng->next_id += (uint32_t) n;
+    } else {
+        // automatic ids continue after the largest explicit one
+        for (int64_t c = 0; c < n; c++) eng->next_id = std::max<uint32_t>(eng->next_id, ids[c] + 1);
+    }
+}
+
+}  // namespace
+
+int gss_db_set(gss_engine *eng, const int32_t *lits, const int64_t *offsets, int64_t n_clauses) {
+    if (!eng || !offsets || n_clauses < 0) return set_error(GSS_ERR_INVALID, "bad arguments to gss_db_set");
+    if (n_clauses > 0xFFFFFFF0LL) return set_error(GSS_ERR_INVALID, "too many clauses (%lld)", (long long) n_clauses);
+    int64_t max_var = -1;
+    GSS_TRY(validate_batch(lits, offsets, n_clauses, max_var));
+    if (n_clauses > 0 && offsets[n_clauses] > 0x7FFFFF00LL)
+        return set_error(GSS_ERR_INVALID, "too many literals (%lld)", (long long) offsets[n_clauses]);
+    eng->h_lits.clear();
+    eng->h_off.assign(1, 0);
+    eng->h_ids.clear();
+    eng->index_of.clear();
+    eng->next_id = 0;
+    mirror_append(eng, lits, offsets, n_clauses, nullptr);
+    GSS_TRY(upload_all(eng));
     eng->max_var = max_var;
     return GSS_OK;
 }
+
+int gss_db_append(gss_engine *eng, const int32_t *lits, const int64_t *offsets, int64_t n_clauses,
+                  const uint32_t *ids) {
+    if (!eng || !offsets || n_clauses < 0) return set_error(GSS_ERR_INVALID, "bad arguments to gss_db_append");
+    if (n_clauses == 0) return GSS_OK;
+    int64_t max_var = -1;
+    GSS_TRY(validate_batch(lits, offsets, n_clauses, max_var));
+    const int64_t first = (int64_t) eng->h_ids.size();
+    if (first + n_clauses > 0xFFFFFFF0LL) return set_error(GSS_ERR_INVALID, "too many clauses");
+    if (ids) {
+        for (int64_t c = 0; c < n_clauses; c++)
+            if (ids[c] < eng->index_of.size() && eng->index_of[ids[c]] != 0xFFFFFFFFu)
+                return set_error(GSS_ERR_INVALID, "clause id %u is already in the database", ids[c]);
+    }
+    const int64_t base = eng->h_off.empty() ? 0 : eng->h_off.back();
+    if (base + offsets[n_clauses] > 0x7FFFFF00LL) return set_error(GSS_ERR_INVALID, "too many literals");
+    mirror_append(eng, lits, offsets, n_clauses, ids);
+    const int64_t n = (int64_t) eng->h_ids.size();
+    const int64_t n_lits = eng->h_off.back();
+    GSS_TRY(ensure_device(eng));
+    GSS_CUDA_TRY(cudaStreamSynchronize(eng->stream));
+    GSS_TRY(eng->lits.grow_keep((n_lits + 8) * sizeof(int32_t), eng->stream, base * sizeof(int32_t)));
+    GSS_TRY(eng->offsets.grow_keep((n + 1) * sizeof(int64_t), eng->stream, (first + 1) * sizeof(int64_t)));
+    GSS_TRY(eng->orig.grow_keep(n * sizeof(uint32_t), eng->stream, first * sizeof(uint32_t)));
+    // new literals, then zero padding past the end
+    std::vector<int32_t> tail(eng->h_lits.begin() + base, eng->h_lits.end());
+    tail.resize(tail.size() + 8, 0);
+    GSS_CUDA_TRY(cudaMemcpy((int32_t *) eng->lits.ptr + base, tail.data(), tail.size() * sizeof(int32_t),
+                            cudaMemcpyHostToDevice));
+    GSS_CUDA_TRY(cudaMemcpy((int64_t *) eng->offsets.ptr + first, eng->h_off.data() + first,
+                            (n - first + 1) * sizeof(int64_t), cudaMemcpyHostToDevice));
+    GSS_CUDA_TRY(cudaMemcpy((uint32_t *) eng->orig.ptr + first, eng->h_ids.data() + first,
+                            (n - first) * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    // alive bits of the new clauses
+    eng->h_alive.resize((n + 31) / 32, 0u);
+    for (int64_t i = first; i < n; i++) eng->h_alive[i >> 5] |= 1u << (i & 31);
+    eng->alive_dirty = true;
+    eng->n_clauses = n;
+    eng->n_lits = n_lits;
+    eng->max_var = std::max(eng->max_var, max_var);
+    eng->tiles_stale = true;
+    return GSS_OK;
+}
+
+int gss_db_delete(gss_engine *eng, const uint32_t *ids, int64_t n) {
+    if (!eng || n < 0 || (n > 0 && !ids)) return set_error(GSS_ERR_INVALID, "bad arguments to gss_db_delete");
+    int64_t missing = 0;
+    for (int64_t k = 0; k < n; k++) {
+        const uint32_t id = ids[k];
+        if (id >= eng->index_of.size() || eng->index_of[id] == 0xFFFFFFFFu) {
+            missing++;
+            continue;
+        }
+        const uint32_t i = eng->index_of[id];
+        if (eng->h_alive[i >> 5] & (1u << (i & 31))) {
+            eng->h_alive[i >> 5] &= ~(1u << (i & 31));
+            eng->n_dead++;
+        }
+        eng->index_of[id] = 0xFFFFFFFFu;
+    }
+    eng->alive_dirty = true;
+    if (missing) return set_error(GSS_ERR_NOT_FOUND, "%lld clause id(s) not in the database", (long long) missing);
+    return GSS_OK;
+}
+
+int gss_db_compact(gss_engine *eng) {
+    if (!eng) return set_error(GSS_ERR_INVALID, "engine is NULL");
+    if (eng->n_dead == 0) return GSS_OK;
+    // the live clauses, re-sorted by length (stable)
+    std::vector<int32_t> lits;
+    std::vector<int64_t> off(1, 0);
+    std::vector<uint32_t> ids;
+    const int64_t n = (int64_t) eng->h_ids.size();
+    for (int64_t i = 0; i < n; i++) {
+        if (!(eng->h_alive[i >> 5] & (1u << (i & 31)))) continue;
+        lits.insert(lits.end(), eng->h_lits.begin() + eng->h_off[i], eng->h_lits.begin() + eng->h_off[i + 1]);
+        off.push_back((int64_t) lits.size());
+        ids.push_back(eng->h_ids[i]);
+    }
+    const uint32_t next = eng->next_id;
+    eng->h_lits.clear();
+    eng->h_off.assign(1, 0);
+    eng->h_ids.clear();
+    std::fill(eng->index_of.begin(), eng->index_of.end(), 0xFFFFFFFFu);
+    mirror_append(eng, lits.data(), off.data(), (int64_t) ids.size(), ids.data());
+    eng->next_id = next;
+    return upload_all(eng);
+}
+
+int64_t gss_db_live_count(const gss_engine *eng) { return eng ? eng->n_clauses - eng->n_dead : -1; }
 
 int64_t gss_db_clause_count(const gss_engine *eng) { return eng ? eng->n_clauses : -1; }
 int64_t gss_db_literal_count(const gss_engine *eng) { return eng ? eng->n_lits : -1; }
@@ -363,6 +537,7 @@ int gss_state_set(gss_engine *eng, const uint32_t *state, int64_t n_vars, int n_
         lpc = 1;
         if (wpl == 1) {
             while (lpc < n_words && lpc < 32) lpc *= 2;
+            if (depth > lpc) depth = lpc;  // a lane group has lpc literals in flight at most
         } else {
             lpc = 32 / wpl;
         }
@@ -425,6 +600,19 @@ int gss_state_set(gss_engine *eng, const uint32_t *state, int64_t n_vars, int n_
     return GSS_OK;
 }
 
+int gss_state_set_start(gss_engine *eng, const uint32_t *start, int n_words) {
+    if (!eng || n_words != eng->n_words || (n_words > 0 && !start))
+        return set_error(GSS_ERR_INVALID, "gss_state_set_start needs the %d words of the current state", eng ? eng->n_words : 0);
+    GSS_TRY(ensure_device(eng));
+    std::vector<uint32_t> st((size_t) eng->n_blocks * eng->state_bw, 0u);
+    memcpy(st.data(), start, n_words * sizeof(uint32_t));
+    if (eng->pass_pending) GSS_CUDA_TRY(cudaStreamSynchronize(eng->stream));
+    GSS_CUDA_TRY(cudaMemcpyAsync(eng->start.ptr, st.data(), st.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                                 eng->stream));
+    GSS_CUDA_TRY(cudaStreamSynchronize(eng->stream));
+    return GSS_OK;
+}
+
 int gss_engine_set_variant(gss_engine *eng, int kind, int lanes_per_clause, int depth, int flags) {
     if (!eng) return set_error(GSS_ERR_INVALID, "engine is NULL");
     if (kind == GSS_KERNEL_AUTO) {
@@ -432,12 +620,14 @@ int gss_engine_set_variant(gss_engine *eng, int kind, int lanes_per_clause, int 
     } else if (kind == GSS_KERNEL_WIDE4 || kind == GSS_KERNEL_WIDE2) {
         const int wpl = words_per_lane(kind);
         const int l = lanes_per_clause ? lanes_per_clause : 32 / wpl;
-        if ((flags & GSS_VARIANT_PIPELINED) ? !valid_wide_pf_variant(wpl, l, depth)
-                                            : !valid_wide_variant(wpl, l, depth, (flags & GSS_VARIANT_OCCUPANCY) ? 1 : 0))
+        if ((flags & GSS_VARIANT_PERSISTENT) ? !valid_wide_persist_variant(wpl, l, depth)
+            : (flags & GSS_VARIANT_PIPELINED) ? !valid_wide_pf_variant(wpl, l, depth)
+                                              : !valid_wide_variant(wpl, l, depth, (flags & GSS_VARIANT_OCCUPANCY) ? 1 : 0))
             return set_error(GSS_ERR_INVALID, "no wide kernel variant for %d words per lane, %d lanes, depth %d", wpl,
                              l, depth);
     } else if (kind == GSS_KERNEL_DIRECT) {
-        if (!valid_variant(lanes_per_clause, depth))
+        if (lanes_per_clause == 0 ? !(depth == 1 || depth == 2 || depth == 4 || depth == 8)
+                                  : !valid_variant(lanes_per_clause, depth))
             return set_error(GSS_ERR_INVALID, "no direct kernel variant for %d lanes per clause, depth %d",
                              lanes_per_clause, depth);
     } else if (kind == GSS_KERNEL_TILED) {
@@ -505,9 +695,25 @@ int launch_pass_into(gss_engine *eng, const void *state, DevBuf &reports, DevBuf
     a.lpc = eng->state_lpc;
     a.g = eng->state_g;
     a.cache_hints = (eng->flags & GSS_VARIANT_L2_HINT) ? 1 : 0;
+    if (eng->state_kind == GSS_KERNEL_TILED) {
+        if (eng->n_dead > 0)
+            return set_error(GSS_ERR_STATE, "the tiled kernel needs a compacted database (gss_db_compact)");
+        if (eng->tiles_stale) GSS_TRY(upload_tiles(eng));
+    }
     a.tile_clause = (const uint32_t *) eng->tile_clause.ptr;
     a.tile_lit = (const uint32_t *) eng->tile_lit.ptr;
     a.n_tiles = eng->n_tiles;
+    a.alive = nullptr;
+    if (eng->n_dead > 0) {
+        if (eng->alive_dirty) {
+            GSS_TRY(eng->alive.reserve(std::max<size_t>(eng->h_alive.size(), 1) * sizeof(uint32_t)));
+            GSS_CUDA_TRY(cudaMemcpyAsync(eng->alive.ptr, eng->h_alive.data(), eng->h_alive.size() * sizeof(uint32_t),
+                                         cudaMemcpyHostToDevice, eng->stream));
+            GSS_CUDA_TRY(cudaStreamSynchronize(eng->stream));  // pageable source
+            eng->alive_dirty = false;
+        }
+        a.alive = (const uint32_t *) eng->alive.ptr;
+    }
     GSS_TRY(eng->err.reserve(sizeof(uint32_t)));
     a.err = (uint32_t *) eng->err.ptr;
     a.start = (const uint32_t *) eng->start.ptr;
@@ -527,16 +733,67 @@ int launch_pass_into(gss_engine *eng, const void *state, DevBuf &reports, DevBuf
             }
         }
     }
+    const bool wide = eng->state_kind == GSS_KERNEL_WIDE4 || eng->state_kind == GSS_KERNEL_WIDE2;
+    if (wide && (eng->flags & GSS_VARIANT_PERSISTENT)) {
+        // arguments through device memory, so the same graph serves every pass
+        GSS_TRY(eng->d_args.reserve(sizeof(CheckArgs)));
+        GSS_TRY(eng->work.reserve(sizeof(uint32_t)));
+        GSS_CUDA_TRY(cudaMemcpyAsync(eng->d_args.ptr, &a, sizeof a, cudaMemcpyHostToDevice, eng->stream));
+        if (ev0) GSS_CUDA_TRY(cudaEventRecord(ev0, eng->stream));
+        auto body = [&]() -> int {
+            GSS_CUDA_TRY(cudaMemsetAsync(a.counts, 0, sizeof(uint32_t) * a.n_parts, eng->stream));
+            GSS_CUDA_TRY(cudaMemsetAsync(a.err, 0, sizeof(uint32_t), eng->stream));
+            GSS_CUDA_TRY(cudaMemsetAsync(eng->work.ptr, 0, sizeof(uint32_t), eng->stream));
+            if (a.n_clauses > 0 && a.n_blocks > 0)
+                GSS_TRY(launch_check_wide_persist((const CheckArgs *) eng->d_args.ptr, words_per_lane(eng->state_kind),
+                                                  eng->state_lpc, eng->state_g, (uint32_t *) eng->work.ptr,
+                                                  eng->stream, eng->sm_count));
+            GSS_CUDA_TRY(cudaMemcpyAsync(h_counts.ptr, counts.ptr, sizeof(uint32_t) * eng->n_parts,
+                                         cudaMemcpyDeviceToHost, eng->stream));
+            GSS_CUDA_TRY(cudaMemcpyAsync((uint32_t *) h_counts.ptr + eng->n_parts, a.err, sizeof(uint32_t),
+                                         cudaMemcpyDeviceToHost, eng->stream));
+            return GSS_OK;
+        };
+        if (eng->use_graph) {
+            const std::vector<uintptr_t> key = {
+                (uintptr_t) a.counts, (uintptr_t) h_counts.ptr, (uintptr_t) a.err, (uintptr_t) eng->work.ptr,
+                (uintptr_t) eng->d_args.ptr, (uintptr_t) eng->state_kind, (uintptr_t) eng->state_lpc,
+                (uintptr_t) eng->state_g, (uintptr_t) eng->n_parts, (uintptr_t) (a.n_clauses > 0 && a.n_blocks > 0)};
+            if (key != eng->graph_key || !eng->graph_exec) {
+                if (eng->graph_exec) cudaGraphExecDestroy(eng->graph_exec);
+                if (eng->graph) cudaGraphDestroy(eng->graph);
+                eng->graph_exec = nullptr;
+                eng->graph = nullptr;
+                GSS_CUDA_TRY(cudaStreamBeginCapture(eng->stream, cudaStreamCaptureModeThreadLocal));
+                const int rc = body();
+                cudaGraph_t g = nullptr;
+                const cudaError_t e = cudaStreamEndCapture(eng->stream, &g);
+                GSS_TRY(rc);
+                if (e != cudaSuccess) return set_error(GSS_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+                eng->graph = g;
+                GSS_CUDA_TRY(cudaGraphInstantiate(&eng->graph_exec, g, 0));
+                eng->graph_key = key;
+                eng->graph_captures++;
+            }
+            GSS_CUDA_TRY(cudaGraphLaunch(eng->graph_exec, eng->stream));
+        } else {
+            GSS_TRY(body());
+        }
+        if (ev1) {
+            GSS_CUDA_TRY(cudaEventRecord(ev1, eng->stream));
+            eng->ev_pending.emplace_back(ev0, ev1);
+        }
+        return GSS_OK;
+    }
     GSS_CUDA_TRY(cudaMemsetAsync(a.counts, 0, sizeof(uint32_t) * a.n_parts, eng->stream));
     GSS_CUDA_TRY(cudaMemsetAsync(a.err, 0, sizeof(uint32_t), eng->stream));
     if (ev0) GSS_CUDA_TRY(cudaEventRecord(ev0, eng->stream));
     if (eng->state_kind == GSS_KERNEL_TILED) {
         GSS_TRY(launch_check_tiled(a, eng->stream, eng->sm_count));
-    } else if ((eng->state_kind == GSS_KERNEL_WIDE4 || eng->state_kind == GSS_KERNEL_WIDE2) &&
-               (eng->flags & GSS_VARIANT_PIPELINED)) {
+    } else if (wide && (eng->flags & GSS_VARIANT_PIPELINED)) {
         GSS_TRY(launch_check_wide_pf(a, words_per_lane(eng->state_kind), (eng->flags & GSS_VARIANT_OCCUPANCY) ? 1 : 0,
                                      eng->stream, eng->sm_count));
-    } else if (eng->state_kind == GSS_KERNEL_WIDE4 || eng->state_kind == GSS_KERNEL_WIDE2) {
+    } else if (wide) {
         GSS_TRY(launch_check_wide(a, words_per_lane(eng->state_kind), (eng->flags & GSS_VARIANT_OCCUPANCY) ? 1 : 0,
                                   eng->stream, eng->sm_count));
     } else {

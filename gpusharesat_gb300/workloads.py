@@ -213,3 +213,47 @@ def make_scale(seed=1, n_vars=2 ** 20, n_clauses=4_000_000, n_solvers=32, plant_
     planted = plant_reports(rng, lits, offsets, state, start, plant_rate)
     return Workload("plain-scale", n_vars, lits, offsets, state, start,
                     np.arange(n_words, dtype=np.int32), n_solvers, planted)
+
+
+def lengths_batching(rng, n, cap=256, a=1.2):
+    """Clause lengths 1 + Zipf(a), at most cap. The shift by one keeps the
+    Zipf shape while leaving out unit clauses (solvers keep units on their
+    trail), which would otherwise report under almost every assignment."""
+    return 1 + lengths_zipf(rng, n, cap=cap - 1, a=a)
+
+
+def batch_starts(rng, n_solvers, lo=4, hi=64):
+    """Started-slot masks for one pass of uneven batches: solver s sends
+    U[lo, hi] assignments, laid out in its two 32-slot words 2s and 2s+1.
+    Returns (start uint32[2 * n_solvers], batch sizes)."""
+    sizes = rng.integers(lo, hi + 1, size=n_solvers)
+    start = np.zeros(2 * n_solvers, dtype=np.uint32)
+    for s, b in enumerate(sizes):
+        b0, b1 = min(int(b), 32), max(int(b) - 32, 0)
+        start[2 * s] = np.uint32((1 << b0) - 1) if b0 < 32 else np.uint32(0xFFFFFFFF)
+        start[2 * s + 1] = np.uint32((1 << b1) - 1)
+    return start, sizes
+
+
+def make_batching(seed=2, n_vars=2 ** 20, n_clauses=8_000_000, n_solvers=48, plant_rate=0.0005):
+    """Batching, uneven: 2^20 variables; 8e6 clauses with lengths 1 + Zipf(1.2)
+    capped at 256; 48 solvers with two 32-slot words each (up to 64
+    assignments per pass), each assignment assigning a uniform 40-90% of the
+    variables with fair signs; 0.05% planted reports. The batch sizes (started
+    slots) are drawn per pass with batch_starts."""
+    rng = np.random.default_rng(seed)
+    lengths = lengths_batching(rng, n_clauses)
+    lits, offsets = distinct_var_clauses(rng, lengths, n_vars)
+    n_words = 2 * n_solvers
+    frac = rng.uniform(0.4, 0.9, size=32 * n_words)
+    state = random_state(rng, n_vars, n_words, frac)
+    start = np.full(n_words, 0xFFFFFFFF, dtype=np.uint32)
+    planted = plant_reports(rng, lits, offsets, state, start, plant_rate)
+    return Workload("batching", n_vars, lits, offsets, state, start,
+                    (np.arange(n_words) // 2).astype(np.int32), n_solvers, planted)
+
+
+def churn_batch(rng, n_vars, n_new):
+    """New clauses of a churn step, from the small workload's generator
+    (lengths 2..30, geometric mean 8)."""
+    return distinct_var_clauses(rng, lengths_small(rng, n_new), n_vars)

@@ -80,6 +80,12 @@ int gss_engine_destroy(gss_engine *eng);
 int gss_engine_set_stream(gss_engine *eng, void *stream);
 /* Number of check-kernel launches so far (for launch accounting). */
 int64_t gss_engine_launch_count(const gss_engine *eng);
+/* With a GSS_VARIANT_PERSISTENT variant: run each pass as one CUDA graph
+ * (counter resets, the kernel, the count readback), captured at the first
+ * pass and replayed while the buffers it names stay the same. */
+int gss_engine_set_graph(gss_engine *eng, int on);
+/* How many times a pass graph was captured (for tests and tuning). */
+int64_t gss_engine_graph_captures(const gss_engine *eng);
 /* When on, each check kernel is bracketed by CUDA events on its stream. */
 int gss_engine_set_timing(gss_engine *eng, int on);
 /* Sum of the bracketed kernel durations since the last call (waits for
@@ -96,6 +102,8 @@ int gss_engine_kernel_time(gss_engine *eng, double *total_ms, int64_t *n_launche
 #define GSS_VARIANT_L2_HINT 1    /* L2 evict-last policy on state loads (direct, tiled) */
 #define GSS_VARIANT_OCCUPANCY 2  /* compile-time register cap: 8 blocks per SM (wide), 4 (pipelined wide) */
 #define GSS_VARIANT_PIPELINED 4  /* wide kinds: next clause's offsets and literals loaded ahead */
+#define GSS_VARIANT_PERSISTENT 8 /* wide kinds: one CTA set for the whole pass, tasks from a work counter,
+                                    arguments from device memory (what gss_engine_set_graph replays) */
 /* Selects the check-kernel variant. A group of lanes_per_clause lanes checks
  * one clause against a slot block of lanes_per_clause x (words per lane)
  * 32-slot words (0 = automatic: one word per lane up to a full warp, or 32
@@ -112,7 +120,21 @@ int gss_engine_set_variant(gss_engine *eng, int kind, int lanes_per_clause, int 
  * least one literal and at most gss_max_clause_len() literals; literals must
  * be non-negative. Synchronous. */
 int gss_db_set(gss_engine *eng, const int32_t *lits, const int64_t *offsets, int64_t n_clauses);
+/* Appends n_clauses clauses (CSR on the host) with the given ids (NULL: the
+ * ids following the largest one used so far, automatic or given). A report's `clause` is
+ * the clause's id; gss_db_set numbers its clauses 0..n-1. Synchronous. */
+int gss_db_append(gss_engine *eng, const int32_t *lits, const int64_t *offsets, int64_t n_clauses,
+                  const uint32_t *ids);
+/* Removes clauses by id: they stop taking part in passes at once (a bit per
+ * clause); their space is reclaimed by gss_db_compact. Unknown ids are
+ * skipped and reported as GSS_ERR_NOT_FOUND after the known ones are removed. */
+int gss_db_delete(gss_engine *eng, const uint32_t *ids, int64_t n);
+/* Rewrites the database without the removed clauses (sorted by length again). */
+int gss_db_compact(gss_engine *eng);
+/* Clauses in the database, removed ones included until a compaction. */
 int64_t gss_db_clause_count(const gss_engine *eng);
+/* Clauses that take part in passes. */
+int64_t gss_db_live_count(const gss_engine *eng);
 int64_t gss_db_literal_count(const gss_engine *eng);
 /* Largest variable index used by the database, -1 if empty. */
 int64_t gss_db_max_var(const gss_engine *eng);
@@ -128,6 +150,11 @@ int gss_max_clause_len(void);
  * The copy is ordered on the engine's stream. */
 int gss_state_set(gss_engine *eng, const uint32_t *state, int64_t n_vars, int n_words,
                   const uint32_t *start, const int32_t *solver_of_word, int on_device);
+
+/* Replaces only the started-slot masks of the current state (n_words must be
+ * the state's word count): a new set of assignment batches over the same
+ * bit planes, without copying the planes again. */
+int gss_state_set_start(gss_engine *eng, const uint32_t *start, int n_words);
 
 /* ---- the check pass (replaces dFindClauses + DReporter::report,
  *      gpuShareLib/GpuRunner.cu:133-177, gpuShareLib/Reporter.cuh:41-58) ---- */

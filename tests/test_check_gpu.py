@@ -178,11 +178,13 @@ TILED_VARIANTS = [(1, l, k, h) for l in (0, 1, 2, 4, 8, 16, 32) for k in (2, 4, 
 WIDE_VARIANTS = [(kind, l, d, occ * 2) for kind, l, ds in ((2, 8, (1, 2, 4)), (2, 4, (1, 2, 4)), (2, 2, (1, 2)),
                                                              (3, 16, (1, 2, 4)), (3, 8, (1, 2, 4)))
                  for d in ds for occ in (0, 1)]
+PERSISTENT_VARIANTS = [(2, 8, d, 8) for d in (1, 2, 4)] + [(2, 4, 2, 8), (2, 2, 2, 8), (3, 16, 2, 8), (3, 8, 2, 8)]
 PIPELINED_VARIANTS = [(kind, l, d, 4 | occ * 2) for kind, l, ds in ((2, 8, (1, 2, 4)), (2, 4, (2, 4)), (3, 16, (2, 4)))
                       for d in ds for occ in (0, 1)]
 
 
-@pytest.mark.parametrize("kind,lpc,depth,hints", DIRECT_VARIANTS + TILED_VARIANTS + WIDE_VARIANTS + PIPELINED_VARIANTS)
+@pytest.mark.parametrize("kind,lpc,depth,hints",
+                         DIRECT_VARIANTS + TILED_VARIANTS + WIDE_VARIANTS + PIPELINED_VARIANTS + PERSISTENT_VARIANTS)
 def test_every_kernel_variant_matches_oracle(engine, kind, lpc, depth, hints):
     """Each kernel variant (kind, lanes per clause, loads in flight or clause
     slots, cache hints) is bit-exact, including slot counts that do not fill
@@ -201,3 +203,91 @@ def test_every_kernel_variant_matches_oracle(engine, kind, lpc, depth, hints):
     finally:
         engine.set_variant()
     _assert_same(gpu, ref, wl)
+
+
+def _live_reference(live, state, start):
+    """Oracle reports of a {id: literals} database, with clause = id."""
+    ids = sorted(live)
+    lits = np.concatenate([np.asarray(live[i], np.int32) for i in ids])
+    offsets = np.zeros(len(ids) + 1, np.int64)
+    offsets[1:] = np.cumsum([len(live[i]) for i in ids])
+    ref = oracle.check(lits, offsets, state, start)
+    ref["clause"] = np.asarray(ids, np.uint32)[ref["clause"]]
+    return np.sort(ref, order=["clause", "word"])
+
+
+@pytest.mark.parametrize("kind", [-1, 0, 2])
+def test_database_churn_matches_oracle(engine, kind):
+    """Deletes (tombstones), appends with ids, and a compaction: every pass
+    reports exactly the live clauses' reports, keyed by clause id."""
+    import gpusharesat_gb300 as g
+    rng = np.random.default_rng(31)
+    base = W.make_scale(seed=31, n_vars=2 ** 12, n_clauses=20000, n_solvers=32)
+    live = {c: base.lits[base.offsets[c]:base.offsets[c + 1]].tolist() for c in range(base.n_clauses)}
+    engine.set_variant(kind, 0, 2, 0)
+    engine.set_db(base.lits, base.offsets)
+    engine.set_state(base.state, base.start, base.solver_of_word)
+    next_id = base.n_clauses
+    for step in range(4):
+        gone = rng.choice(sorted(live), size=1000, replace=False)
+        engine.delete(gone)
+        for i in gone:
+            del live[int(i)]
+        lengths = W.lengths_small(rng, 1000)
+        lits, offs = W.distinct_var_clauses(rng, lengths, base.n_vars)
+        ids = np.arange(next_id, next_id + 1000) if step % 2 else None
+        engine.append_db(lits, offs, ids)
+        for k in range(1000):
+            live[next_id + k] = lits[offs[k]:offs[k + 1]].tolist()
+        next_id += 1000
+        if step == 2:
+            engine.compact()
+            assert engine.clause_count == len(live)
+        assert engine.live_count == len(live)
+        got = np.sort(engine.check(), order=["clause", "word"])
+        ref = _live_reference(live, base.state, base.start)
+        assert len(got) == len(ref)
+        for f in ("clause", "word", "mask"):
+            np.testing.assert_array_equal(got[f], ref[f])
+    with pytest.raises(g.GssError):
+        engine.delete([10 ** 8])
+    engine.set_variant()
+
+
+def test_persistent_graph_replays_across_passes(engine):
+    """The persistent kernel run as a captured graph: one capture serves
+    passes whose database and assignments change; every pass is exact."""
+    import gpusharesat_gb300 as g
+    rng = np.random.default_rng(41)
+    base = W.make_scale(seed=41, n_vars=2 ** 12, n_clauses=20000, n_solvers=40)
+    live = {c: base.lits[base.offsets[c]:base.offsets[c + 1]].tolist() for c in range(base.n_clauses)}
+    engine.set_variant(g.KERNEL_WIDE4, 8, 2, g.VARIANT_PERSISTENT)
+    engine.set_graph(True)
+    try:
+        engine.set_db(base.lits, base.offsets)
+        engine.set_capacity(1 << 22)
+        captures0 = engine.graph_captures
+        next_id = base.n_clauses
+        for step in range(3):
+            state = W.random_state(rng, base.n_vars, base.n_words, rng.uniform(0.4, 0.9, 32 * base.n_words))
+            start = rng.integers(0, 2 ** 32, size=base.n_words, dtype=np.uint32)
+            engine.set_state(state, start, base.solver_of_word)
+            gone = rng.choice(sorted(live), size=500, replace=False)
+            engine.delete(gone)
+            for i in gone:
+                del live[int(i)]
+            lits, offs = W.distinct_var_clauses(rng, W.lengths_small(rng, 500), base.n_vars)
+            engine.append_db(lits, offs)
+            for k in range(500):
+                live[next_id + k] = lits[offs[k]:offs[k + 1]].tolist()
+            next_id += 500
+            got = np.sort(engine.check(), order=["clause", "word"])
+            ref = _live_reference(live, state, start)
+            assert len(got) == len(ref)
+            for f in ("clause", "word", "mask"):
+                np.testing.assert_array_equal(got[f], ref[f])
+        assert engine.graph_captures - captures0 == 1
+    finally:
+        engine.set_graph(False)
+        engine.set_capacity(0)
+        engine.set_variant()
