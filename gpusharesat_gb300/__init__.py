@@ -327,6 +327,10 @@ def _sharer_sigs(lib):
     _sig(lib, "gss_sharer_current_assignment", c_int, vp, c_int, vp)
     _sig(lib, "gss_sharer_set_max_clause_len", c_int, vp, c_int)
     _sig(lib, "gss_sharer_set_variant", c_int, vp, c_int, c_int, c_int, c_int)
+    _sig(lib, "gss_sharer_set_clause_budget", c_int, vp, c_i64)
+    _sig(lib, "gss_sharer_evicted_count", c_i64, vp)
+    _sig(lib, "gss_sharer_device_compactions", c_i64, vp)
+    _sig(lib, "gss_serving_run", c_int, vp, vp)
     _sig(lib, "gss_activity_create", vp, ctypes.c_float)
     _sig(lib, "gss_activity_destroy", None, vp)
     _sig(lib, "gss_activity_add", c_i64, vp, c_int)
@@ -466,6 +470,55 @@ class ClauseSharer:
 
     def setVariant(self, kind=-1, lanes_per_clause=0, depth=2, flags=0):
         _check(self.lib.gss_sharer_set_variant(self.h, kind, lanes_per_clause, depth, flags))
+
+    def setClauseBudget(self, max_clauses):
+        """HBM budget: a pass checks at most max_clauses live clauses; the
+        oldest clauses not reported in the last 8 passes are evicted first.
+        0 = no budget."""
+        _check(self.lib.gss_sharer_set_clause_budget(self.h, int(max_clauses)))
+
+    def evictedCount(self):
+        return int(self.lib.gss_sharer_evicted_count(self.h))
+
+    def deviceCompactions(self):
+        return int(self.lib.gss_sharer_device_compactions(self.h))
+
+
+class ServingParams(ctypes.Structure):
+    """gss_serving_params: one run of the serving load generator."""
+    _fields_ = [("seconds", ctypes.c_double), ("warmup_seconds", ctypes.c_double),
+                ("assign_rate", ctypes.c_double), ("n_solvers", ctypes.c_int), ("n_vars", ctypes.c_int),
+                ("budget", ctypes.c_int64), ("initial_clauses", ctypes.c_int64),
+                ("clause_rate", ctypes.c_double), ("plant_rate", ctypes.c_double),
+                ("batch_max", ctypes.c_int), ("trail_fraction", ctypes.c_double),
+                ("trail_change", ctypes.c_int), ("seed", ctypes.c_uint64)]
+
+
+class ServingResult(ctypes.Structure):
+    _fields_ = [("p50_ms", ctypes.c_double), ("p99_ms", ctypes.c_double), ("p999_ms", ctypes.c_double),
+                ("mean_ms", ctypes.c_double), ("max_ms", ctypes.c_double),
+                ("assignments", ctypes.c_int64), ("reports_popped", ctypes.c_int64), ("passes", ctypes.c_int64),
+                ("checks_per_s", ctypes.c_double), ("assignments_per_s", ctypes.c_double),
+                ("elapsed_s", ctypes.c_double), ("evicted", ctypes.c_int64), ("retries", ctypes.c_int64),
+                ("clauses_streamed", ctypes.c_int64), ("live_clauses_end", ctypes.c_int64),
+                ("device_compactions", ctypes.c_int64)]
+
+
+def serving_run(**params):
+    """Runs the serving load generator on the current CUDA device; returns its
+    result as a dict. Keys of params: the fields of ServingParams."""
+    lib = load()
+    _sharer_sigs(lib)
+    p = ServingParams(seconds=5.0, warmup_seconds=1.0, assign_rate=5e4, n_solvers=64, n_vars=2 ** 21,
+                      budget=0, initial_clauses=1_000_000, clause_rate=2e5, plant_rate=0.01, batch_max=32,
+                      trail_fraction=0.5, trail_change=4, seed=1)
+    for k, v in params.items():
+        if not hasattr(p, k):
+            raise KeyError(k)
+        setattr(p, k, v)
+    r = ServingResult()
+    _check(lib.gss_serving_run(ctypes.byref(p), ctypes.byref(r)))
+    return {name: getattr(r, name) for name, _ in ServingResult._fields_}
 
 
 class ClauseActivity:

@@ -5,6 +5,7 @@ measures the other configurations of the same metric, each against its own
 baseline, and prints one JSON line per pass plus a summary line:
 
     python -m gpusharesat_gb300.bench_configs batching [--clauses 8000000 --passes 6]
+    python -m gpusharesat_gb300.bench_configs serving [--rates 5e4 1e5 2e5 --budget 16000000]
 
 batching: 8e6 clauses (lengths 1 + Zipf(1.2), at most 256), 48 solvers sending
     uneven batches of 4..64 assignments per pass (two 32-slot words each), 5%
@@ -16,6 +17,14 @@ batching: 8e6 clauses (lengths 1 + Zipf(1.2), at most 256), 48 solvers sending
                   as a captured CUDA graph
     The reports of `batched` and `single` are compared record for record on
     the first pass, and the union of the per-solver launches with `single`'s.
+
+serving: 2^21 variables; 64 solver threads with trails of half the variables
+    send assignments (each unsets and sets 1..8 literals) in Poisson batches
+    of 1..32 at an aggregate 5e4, 1e5 and 2e5 assignments/s; a clause stream
+    of 2e5 clauses/s (lengths 1 + Zipf(1.2), at most 256; 0.05% planted to
+    report) flows into an HBM budget of 16e6 clauses, full from the start.
+    Reports p50/p99/p999 latency from an assignment's arrival to the moment
+    every report of it is delivered, and sustained checks/s.
 """
 import argparse
 import json
@@ -136,15 +145,45 @@ def batching(args):
     return summary
 
 
+def serving(args):
+    """The serving loop through the sharer's C ABI, driven by the C++ load
+    generator (gss_serving_run): 64 solver threads, Poisson batches of 1..32
+    assignments at an aggregate rate, a clause stream into an HBM budget.
+    Each rate is a fresh sharer with the same seed."""
+    rows = []
+    for rate in args.rates:
+        t0 = time.time()
+        r = g.serving_run(seconds=args.seconds, warmup_seconds=args.warmup_seconds, assign_rate=rate,
+                          n_solvers=64, n_vars=2 ** 21, budget=args.budget, initial_clauses=args.budget,
+                          clause_rate=2e5, plant_rate=0.0005, batch_max=32, trail_fraction=0.5,
+                          trail_change=8, seed=3)
+        r.update({"config": "serving", "assign_rate": rate, "budget": args.budget,
+                  "wall_s": round(time.time() - t0, 1)})
+        rows.append(r)
+        print(json.dumps(r), flush=True)
+    summary = {"config": "serving", "rates": args.rates,
+               "p50_ms": [r["p50_ms"] for r in rows], "p99_ms": [r["p99_ms"] for r in rows],
+               "p999_ms": [r["p999_ms"] for r in rows], "checks_per_s": [r["checks_per_s"] for r in rows],
+               "assignments_per_s": [r["assignments_per_s"] for r in rows]}
+    print(json.dumps(summary), flush=True)
+    return summary
+
+
 def main(argv=None):
     p = argparse.ArgumentParser()
-    p.add_argument("config", choices=["batching"])
+    p.add_argument("config", choices=["batching", "serving"])
     p.add_argument("--clauses", type=int, default=8_000_000)
     p.add_argument("--passes", type=int, default=6)
+    p.add_argument("--rates", type=float, nargs="+", default=[5e4, 1e5, 2e5])
+    p.add_argument("--budget", type=int, default=16_000_000)
+    p.add_argument("--seconds", type=float, default=10.0)
+    p.add_argument("--warmup-seconds", type=float, default=2.0)
     args = p.parse_args(argv)
     build.build()
     if args.config == "batching":
         batching(args)
+    elif args.config == "serving":
+        serving(args)
 
 
 if __name__ == "__main__":

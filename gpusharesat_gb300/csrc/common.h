@@ -21,6 +21,10 @@ constexpr int kMaxClauseLen = 4096;
 constexpr int kTileLits = 512;
 constexpr int kBufLits = kTileLits + 8;
 
+// Zero literals after the last clause: kernels that read a few literals ahead
+// stay inside the buffer.
+constexpr int kClausePad = 8;
+
 // Sets the calling thread's error message and returns `code`.
 int set_error(int code, const char *fmt, ...);
 
@@ -84,12 +88,32 @@ struct CheckArgs {
     uint32_t n_tiles;
     uint32_t *err;                // device flag, set to nonzero when a bounded wait gives up
     const uint32_t *alive;        // device, 1 bit per clause (NULL: every clause is live)
+    uint32_t alive_by_id;         // alive is indexed by orig[c] rather than by c
 };
 
 // Whether clause c of the database takes part in the pass.
 __device__ __forceinline__ bool clause_live(const CheckArgs &a, uint32_t c) {
-    return a.alive == nullptr || ((__ldg(a.alive + (c >> 5)) >> (c & 31)) & 1u);
+    if (a.alive == nullptr) return true;
+    const uint32_t i = a.alive_by_id ? __ldg(a.orig + c) : c;
+    return (__ldg(a.alive + (i >> 5)) >> (i & 31)) & 1u;
 }
+
+// Order-preserving device compaction of a CSR clause database: keeps the
+// clauses whose id (ids[c]) has its bit set in `alive`.
+struct CompactArgs {
+    const int32_t *lits;
+    const int64_t *offsets;  // n_clauses + 1
+    const uint32_t *ids;
+    uint32_t n_clauses;
+    const uint32_t *alive;   // bit per id
+    int32_t *new_lits;       // room for the live literals + kClausePad
+    int64_t *new_offsets;    // room for n_clauses + 1
+    uint32_t *new_ids;       // room for n_clauses
+    void *scratch;           // compact_scratch_bytes(n_clauses), 256-byte aligned
+};
+size_t compact_scratch_bytes(uint32_t n_clauses);
+// Synchronizes `stream`; returns the live clause and literal counts.
+int compact_by_id(const CompactArgs &a, cudaStream_t stream, int sm_count, uint32_t *n_out, int64_t *lits_out);
 
 // Launches the check kernel on `stream` (the counters must already be zero).
 // Returns a GSS status.

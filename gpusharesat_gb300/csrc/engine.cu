@@ -685,6 +685,7 @@ int launch_pass_into(gss_engine *eng, const void *state, DevBuf &reports, DevBuf
     if (eng->state_kind == GSS_KERNEL_DIRECT && !valid_variant(eng->state_lpc, eng->state_g) && eng->n_words > 0)
         return set_error(GSS_ERR_STATE, "no direct kernel variant for %d lanes per clause", eng->state_lpc);
     CheckArgs a;
+    memset(&a, 0, sizeof a);
     a.lits = (const int32_t *) eng->lits.ptr;
     a.offsets = (const int64_t *) eng->offsets.ptr;
     a.orig = (const uint32_t *) eng->orig.ptr;

@@ -505,16 +505,16 @@ int Sharer::ensure_state() {
 }
 
 int Sharer::upload_db() {
-    // whole database (after reduceDb): length-sorted device order
+    // whole database (after reduceDb or a host compaction): meta_ order
     const uint32_t n = (uint32_t) meta_.size();
-    h_offsets_.assign(n + 1, 0);
-    for (uint32_t i = 0; i < n; i++) h_offsets_[i + 1] = h_offsets_[i] + meta_[i].len;
-    std::vector<int32_t> lits(h_offsets_[n] + 8, 0);
+    std::vector<int64_t> offsets(n + 1, 0);
+    for (uint32_t i = 0; i < n; i++) offsets[i + 1] = offsets[i] + meta_[i].len;
+    std::vector<int32_t> lits(offsets[n] + kClausePad, 0);
     for (uint32_t i = 0; i < n; i++)
-        memcpy(&lits[h_offsets_[i]], &h_lits_[meta_[i].lit_off], meta_[i].len * sizeof(int32_t));
+        memcpy(&lits[offsets[i]], &h_lits_[meta_[i].lit_off], meta_[i].len * sizeof(int32_t));
     // compact the host arena to the device order
-    h_lits_.assign(lits.begin(), lits.begin() + h_offsets_[n]);
-    for (uint32_t i = 0; i < n; i++) meta_[i].lit_off = (uint32_t) h_offsets_[i];
+    h_lits_.assign(lits.begin(), lits.begin() + offsets[n]);
+    for (uint32_t i = 0; i < n; i++) meta_[i].lit_off = (uint32_t) offsets[i];
     std::vector<uint32_t> orig(std::max<uint32_t>(n, 1));
     for (uint32_t i = 0; i < n; i++) orig[i] = i;
     GSS_TRY(d_lits_.reserve(lits.size() * sizeof(int32_t)));
@@ -522,12 +522,147 @@ int Sharer::upload_db() {
     GSS_TRY(d_orig_.reserve(orig.size() * sizeof(uint32_t)));
     GSS_CUDA_TRY(cudaMemcpyAsync(d_lits_.ptr, lits.data(), lits.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
                                  stream_));
-    GSS_CUDA_TRY(cudaMemcpyAsync(d_offsets_.ptr, h_offsets_.data(), (n + 1) * sizeof(int64_t),
+    GSS_CUDA_TRY(cudaMemcpyAsync(d_offsets_.ptr, offsets.data(), (n + 1) * sizeof(int64_t),
                                  cudaMemcpyHostToDevice, stream_));
     GSS_CUDA_TRY(cudaMemcpyAsync(d_orig_.ptr, orig.data(), orig.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
                                  stream_));
     GSS_CUDA_TRY(cudaStreamSynchronize(stream_));
     dev_clauses_ = n;
+    dev_lits_ = offsets[n];
+    h_alive_.assign((n + 31) / 32, ~0u);
+    n_dead_ = 0;
+    dev_dead_ = 0;
+    evict_cursor_ = 0;
+    alive_synced_ = false;
+    alive_lo_ = SIZE_MAX;
+    alive_hi_ = 0;
+    return GSS_OK;
+}
+
+void Sharer::mark_alive(size_t lo_word, size_t hi_word) {
+    alive_lo_ = std::min(alive_lo_, lo_word);
+    alive_hi_ = std::max(alive_hi_, hi_word);
+}
+
+int Sharer::sync_alive() {
+    // Brings d_alive_ up to h_alive_: all of it the first time, then the
+    // words changed since (evictions take the oldest clauses, appends add at
+    // the end, so the range stays short).
+    const size_t words = std::max<size_t>(h_alive_.size(), 1);
+    if (!alive_synced_) {
+        alive_lo_ = 0;
+        alive_hi_ = h_alive_.size();
+    }
+    if (d_alive_.bytes < words * sizeof(uint32_t)) {
+        GSS_TRY(d_alive_.grow_keep(words * sizeof(uint32_t), stream_,
+                                   alive_synced_ ? std::min(d_alive_.bytes, words * sizeof(uint32_t)) : 0));
+    }
+    alive_hi_ = std::min(alive_hi_, h_alive_.size());
+    if (alive_lo_ < alive_hi_) {
+        GSS_CUDA_TRY(cudaMemcpyAsync((uint32_t *) d_alive_.ptr + alive_lo_, h_alive_.data() + alive_lo_,
+                                     (alive_hi_ - alive_lo_) * sizeof(uint32_t), cudaMemcpyHostToDevice, stream_));
+        GSS_CUDA_TRY(cudaStreamSynchronize(stream_));  // pageable source
+    }
+    alive_synced_ = true;
+    alive_lo_ = SIZE_MAX;
+    alive_hi_ = 0;
+    return GSS_OK;
+}
+
+int Sharer::compact_device() {
+    // drops evicted clauses from the device arrays (order kept, on the GPU)
+    GSS_TRY(sync_alive());
+    const uint32_t n = dev_clauses_;
+    const int64_t live_lits = dev_lits_;  // an upper bound on what stays
+    GSS_TRY(d_lits2_.reserve((size_t) (live_lits + kClausePad) * sizeof(int32_t)));
+    GSS_TRY(d_offsets2_.reserve(((size_t) n + 1) * sizeof(int64_t)));
+    GSS_TRY(d_orig2_.reserve(std::max<size_t>(n, 1) * sizeof(uint32_t)));
+    GSS_TRY(d_compact_.reserve(compact_scratch_bytes(n)));
+    CompactArgs c;
+    c.lits = (const int32_t *) d_lits_.ptr;
+    c.offsets = (const int64_t *) d_offsets_.ptr;
+    c.ids = (const uint32_t *) d_orig_.ptr;
+    c.n_clauses = n;
+    c.alive = (const uint32_t *) d_alive_.ptr;
+    c.new_lits = (int32_t *) d_lits2_.ptr;
+    c.new_offsets = (int64_t *) d_offsets2_.ptr;
+    c.new_ids = (uint32_t *) d_orig2_.ptr;
+    c.scratch = d_compact_.ptr;
+    uint32_t kept;
+    int64_t kept_lits;
+    GSS_TRY(compact_by_id(c, stream_, sm_count_, &kept, &kept_lits));
+    for (auto bufs : {std::make_pair(&d_lits_, &d_lits2_), std::make_pair(&d_offsets_, &d_offsets2_),
+                      std::make_pair(&d_orig_, &d_orig2_)}) {
+        std::swap(bufs.first->ptr, bufs.second->ptr);
+        std::swap(bufs.first->bytes, bufs.second->bytes);
+    }
+    dev_clauses_ = kept;
+    dev_lits_ = kept_lits;
+    dev_dead_ = 0;
+    device_compactions_++;
+    return GSS_OK;
+}
+
+void Sharer::evict(int64_t n) {
+    // Oldest first among the clauses not reported in the last kRecentPasses
+    // passes; then, if that is not enough, the oldest of the rest. Age is the
+    // device order: arrival order, except that a reduceDb sorts its survivors
+    // by length. evict_cursor_ is the oldest live clause that round 0 may
+    // still take (the oldest one it skipped as recently reported, or the one
+    // after the last it took).
+    constexpr int32_t kRecentPasses = 8;
+    auto live = [&](size_t i) { return (h_alive_[i >> 5] >> (i & 31)) & 1u; };
+    auto take = [&](size_t i) {
+        h_alive_[i >> 5] &= ~(1u << (i & 31));
+        mark_alive(i >> 5, (i >> 5) + 1);
+        n_dead_++;
+        dev_dead_++;
+        evicted_++;
+        stats_[kGpuClauses]--;
+        stats_[kGpuClauseLengthSum] -= meta_[i].len;
+    };
+    size_t first_skipped = SIZE_MAX;
+    size_t i = evict_cursor_;
+    for (; i < meta_.size() && n > 0; i++) {
+        if (h_alive_[i >> 5] == 0) {  // a whole word of tombstones
+            i |= 31;
+            continue;
+        }
+        if (!live(i)) continue;
+        const ClauseMeta &m = meta_[i];
+        if (m.last_report >= 0 && pass_no_ - m.last_report <= kRecentPasses) {
+            first_skipped = std::min(first_skipped, i);
+            continue;
+        }
+        take(i);
+        n--;
+    }
+    evict_cursor_ = std::min(first_skipped, i);
+    for (size_t j = 0; j < meta_.size() && n > 0; j++) {
+        if (!live(j)) continue;
+        take(j);
+        n--;
+    }
+}
+
+int Sharer::compact(bool upload) {
+    // drops evicted clauses from meta_ and the activities, keeping the order
+    // (and so the age order); upload = rebuild the device database too
+    std::vector<uint8_t> keep(meta_.size(), 0);
+    std::vector<ClauseMeta> kept;
+    kept.reserve(meta_.size() - n_dead_);
+    for (size_t i = 0; i < meta_.size(); i++) {
+        if (h_alive_[i >> 5] & (1u << (i & 31))) {
+            keep[i] = 1;
+            kept.push_back(meta_[i]);
+        }
+    }
+    act_->compact(keep);
+    meta_.swap(kept);
+    if (upload) return upload_db();
+    h_alive_.assign((meta_.size() + 31) / 32, ~0u);
+    n_dead_ = 0;
+    evict_cursor_ = 0;
     return GSS_OK;
 }
 
@@ -552,6 +687,7 @@ int Sharer::append_clauses(std::vector<int64_t> &ids, std::vector<int32_t> &lits
         m.gpu_id = ids[i];
         m.len = lens[i];
         m.lit_off = 0;
+        m.last_report = -1;
         meta_.push_back(m);
         stats_[kGpuClausesAdded]++;
         stats_[kGpuClauses]++;
@@ -560,12 +696,14 @@ int Sharer::append_clauses(std::vector<int64_t> &ids, std::vector<int32_t> &lits
     // device order of this batch: by length (warps then check equal lengths)
     std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return lens[a] < lens[b]; });
     std::vector<ClauseMeta> sorted(ids.size());
-    const int64_t base_off = h_offsets_.empty() ? 0 : h_offsets_.back();
-    if (h_offsets_.empty()) h_offsets_.push_back(0);
+    // the new clauses go after the device's last clause
+    const int64_t base_off = dev_lits_;
+    const uint32_t dpos = dev_clauses_;
     std::vector<int32_t> new_lits;
-    new_lits.reserve(off + 8);
+    new_lits.reserve(off + kClausePad);
     std::vector<int64_t> new_offsets;
     new_offsets.reserve(ids.size());
+    int64_t end_off = base_off;
     for (size_t k = 0; k < order.size(); k++) {
         const size_t i = order[k];
         ClauseMeta m = meta_[first + i];
@@ -573,34 +711,38 @@ int Sharer::append_clauses(std::vector<int64_t> &ids, std::vector<int32_t> &lits
         h_lits_.insert(h_lits_.end(), lits.begin() + starts[i], lits.begin() + starts[i] + lens[i]);
         new_lits.insert(new_lits.end(), lits.begin() + starts[i], lits.begin() + starts[i] + lens[i]);
         sorted[k] = m;
-        h_offsets_.push_back(h_offsets_.back() + lens[i]);
-        new_offsets.push_back(h_offsets_.back());
+        end_off += lens[i];
+        new_offsets.push_back(end_off);
     }
     std::copy(sorted.begin(), sorted.end(), meta_.begin() + first);
     std::vector<uint32_t> order32(order.begin(), order.end());
     act_->permute_tail(first, order32);
-    new_lits.resize(off + 8, 0);
+    new_lits.resize(off + kClausePad, 0);
     const uint32_t n = (uint32_t) meta_.size();
-    const int64_t n_lits = h_offsets_.back();
-    if (n_lits > 0x7FFFFF00LL) return set_error(GSS_ERR_NOMEM, "clause database exceeds 2^31 literals");
+    const uint32_t n_dev = dpos + (uint32_t) ids.size();
+    if (end_off > 0x7FFFFF00LL) return set_error(GSS_ERR_NOMEM, "clause database exceeds 2^31 literals");
     // grow the device arrays, keeping their contents
-    GSS_TRY(d_lits_.grow_keep((n_lits + 8) * sizeof(int32_t), stream_, base_off * sizeof(int32_t)));
-    GSS_TRY(d_offsets_.grow_keep((n + 1) * sizeof(int64_t), stream_, (first + 1) * sizeof(int64_t)));
-    GSS_TRY(d_orig_.grow_keep(n * sizeof(uint32_t), stream_, first * sizeof(uint32_t)));
+    GSS_TRY(d_lits_.grow_keep((end_off + kClausePad) * sizeof(int32_t), stream_, base_off * sizeof(int32_t)));
+    GSS_TRY(d_offsets_.grow_keep((n_dev + 1) * sizeof(int64_t), stream_, (dpos + 1) * sizeof(int64_t)));
+    GSS_TRY(d_orig_.grow_keep(n_dev * sizeof(uint32_t), stream_, dpos * sizeof(uint32_t)));
     std::vector<uint32_t> orig(ids.size());
     for (size_t k = 0; k < ids.size(); k++) orig[k] = (uint32_t) (first + k);
     GSS_CUDA_TRY(cudaMemcpyAsync((int32_t *) d_lits_.ptr + base_off, new_lits.data(), new_lits.size() * sizeof(int32_t),
                                  cudaMemcpyHostToDevice, stream_));
-    if (first == 0) {
+    if (dpos == 0) {
         int64_t zero = 0;
         GSS_CUDA_TRY(cudaMemcpyAsync(d_offsets_.ptr, &zero, sizeof(int64_t), cudaMemcpyHostToDevice, stream_));
     }
-    GSS_CUDA_TRY(cudaMemcpyAsync((int64_t *) d_offsets_.ptr + first + 1, new_offsets.data(),
+    GSS_CUDA_TRY(cudaMemcpyAsync((int64_t *) d_offsets_.ptr + dpos + 1, new_offsets.data(),
                                  new_offsets.size() * sizeof(int64_t), cudaMemcpyHostToDevice, stream_));
-    GSS_CUDA_TRY(cudaMemcpyAsync((uint32_t *) d_orig_.ptr + first, orig.data(), orig.size() * sizeof(uint32_t),
+    GSS_CUDA_TRY(cudaMemcpyAsync((uint32_t *) d_orig_.ptr + dpos, orig.data(), orig.size() * sizeof(uint32_t),
                                  cudaMemcpyHostToDevice, stream_));
     GSS_CUDA_TRY(cudaStreamSynchronize(stream_));  // the host vectors above are pageable
-    dev_clauses_ = n;
+    dev_clauses_ = n_dev;
+    dev_lits_ = end_off;
+    h_alive_.resize((n + 31) / 32, 0u);
+    for (size_t i = first; i < n; i++) h_alive_[i >> 5] |= 1u << (i & 31);
+    mark_alive(first >> 5, h_alive_.size());
     return GSS_OK;
 }
 
@@ -638,6 +780,13 @@ int Sharer::run_check(Pass &p) {
     a.g = eff_depth_;
     a.cache_hints = (flags_ & GSS_VARIANT_L2_HINT) ? 1 : 0;
     a.err = (uint32_t *) d_err_.ptr;
+    a.alive = nullptr;
+    if (dev_dead_ > 0) {
+        // evicted clauses still on the device: skipped through the bitmap
+        GSS_TRY(sync_alive());
+        a.alive = (const uint32_t *) d_alive_.ptr;
+        a.alive_by_id = 1;
+    }
     GSS_CUDA_TRY(cudaMemsetAsync(a.counts, 0, sizeof(uint32_t) * n_parts_, stream_));
     GSS_CUDA_TRY(cudaMemsetAsync(a.err, 0, sizeof(uint32_t), stream_));
     if (p.active_words > 0 && p.n_clauses > 0) {
@@ -710,7 +859,11 @@ int Sharer::gather() {
     stats_[kClauseTestsOnGroups] += p.n_clauses;
     stats_[kClauseTestsOnAssigs] += (int64_t) p.n_clauses * p.active_words;
     stats_[kGpuReports] += (int64_t) h_reports_.size();
-    for (const gss_report &r : h_reports_) act_->bump(r.clause);
+    for (const gss_report &r : h_reports_) {
+        act_->bump(r.clause);
+        meta_[r.clause].last_report = pass_no_;
+    }
+    pass_no_++;
     const int64_t t1 = now_us();
     // Reported::fill (gpuShareLib/Reported.cu:160-204): a batch for every
     // solver that had assignments in the pass, reported or not.
@@ -756,6 +909,13 @@ int Sharer::launch_pass() {
         int rc = append_clauses(ids, lits, lens);
         if (rc == GSS_ERR_NOMEM) out_of_memory_ = true;
         GSS_TRY(rc);
+    }
+    if (budget_ > 0 && live_clauses() > budget_) {
+        evict(live_clauses() - budget_);
+        if (n_dead_ * 2 > (int64_t) meta_.size())
+            GSS_TRY(compact());  // host tombstones: rebuild everything
+        else if (dev_dead_ * 5 > (int64_t) dev_clauses_)
+            GSS_TRY(compact_device());
     }
     if (stats_[kGpuClauses] == 0) return GSS_OK;  // nothing to check: assignments wait
     GSS_TRY(ensure_state());
@@ -832,6 +992,7 @@ int Sharer::reduce_db() {
     // ones with lbd < 100 whose activity reaches the median estimate.
     GSS_CUDA_TRY(cudaSetDevice(device_));
     if (pass_.pending) GSS_TRY(gather());
+    if (n_dead_ > 0) GSS_TRY(compact(false));  // the upload below rebuilds the device side
     const int64_t t0 = now_us();
     added_at_last_reduce_ = stats_[kGpuClausesAdded];
     stats_[kGpuReduceDbs]++;
@@ -886,6 +1047,7 @@ int Sharer::write_cnf(FILE *f) {
     for (size_t i = 0; i < order.size(); i++) order[i] = i;
     std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return meta_[a].len < meta_[b].len; });
     for (size_t i : order) {
+        if (!(h_alive_[i >> 5] & (1u << (i & 31)))) continue;
         const ClauseMeta &m = meta_[i];
         for (uint32_t k = 0; k < m.len; k++) {
             const int32_t l = h_lits_[m.lit_off + k];
@@ -1057,6 +1219,16 @@ int gss_sharer_set_max_clause_len(gss_sharer *s, int n) {
     s->impl->set_max_clause_len(n);
     return GSS_OK;
 }
+
+int gss_sharer_set_clause_budget(gss_sharer *s, int64_t max_clauses) {
+    GSS_SHARER(s);
+    if (max_clauses < 0) return gss::set_error(GSS_ERR_INVALID, "negative clause budget");
+    s->impl->set_clause_budget(max_clauses);
+    return GSS_OK;
+}
+
+int64_t gss_sharer_evicted_count(gss_sharer *s) { return s ? s->impl->evicted() : -1; }
+int64_t gss_sharer_device_compactions(gss_sharer *s) { return s ? s->impl->device_compactions() : -1; }
 
 int gss_sharer_set_variant(gss_sharer *s, int kind, int lanes_per_clause, int depth, int flags) {
     GSS_SHARER(s);

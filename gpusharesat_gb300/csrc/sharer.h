@@ -119,8 +119,9 @@ struct SolverReported {
 // Sharer::act_ (both are kept in device order).
 struct ClauseMeta {
     int64_t gpu_id;
-    uint32_t lit_off;  // into the host literal arena
+    uint32_t lit_off;      // into the host literal arena
     uint32_t len;
+    int32_t last_report;   // pass of its last report, -1 if never reported
 };
 
 struct Options {
@@ -158,6 +159,10 @@ public:
     int max_clause_len() const { return max_len_; }
     void set_max_clause_len(int n) { max_len_ = n; }
     int set_variant(int kind, int lpc, int depth, int flags);
+    void set_clause_budget(int64_t n) { budget_ = n; }
+    int64_t evicted() const { return evicted_; }
+    int64_t device_compactions() const { return device_compactions_; }
+    int64_t live_clauses() const { return (int64_t) meta_.size() - n_dead_; }
 
 private:
     struct Pass {
@@ -177,6 +182,11 @@ private:
     int ensure_state();
     int append_clauses(std::vector<int64_t> &ids, std::vector<int32_t> &lits, std::vector<uint32_t> &lens);
     int upload_db();
+    void evict(int64_t n);
+    int compact(bool upload = true);
+    int compact_device();
+    int sync_alive();
+    void mark_alive(size_t lo_word, size_t hi_word);
     void unset_pending_locked(int solver);
     void log(int level, const std::string &msg) const;
 
@@ -204,10 +214,31 @@ private:
     std::unique_ptr<ClauseActivity> act_;
     int64_t added_at_last_reduce_ = 0;
     bool out_of_memory_ = false;
+    // Device database: CSR of the clauses in device order, and d_orig_, the
+    // index in meta_ of each (the id reports carry). Device order is meta_
+    // order with evicted clauses compacted away.
     DevBuf d_lits_, d_offsets_, d_orig_;
-    std::vector<int64_t> h_offsets_;
+    DevBuf d_lits2_, d_offsets2_, d_orig2_, d_compact_;  // compaction targets, swapped in
+    int64_t dev_lits_ = 0;
     uint32_t dev_clauses_ = 0;
     int64_t max_var_ = -1;
+    // HBM budget: the oldest clauses not reported in the last kRecentPasses
+    // passes are evicted. An evicted clause keeps its meta_ entry (a
+    // tombstone: its bit in h_alive_ is clear) until a reduceDb or until
+    // tombstones are half of meta_; on the device it is skipped through the
+    // bitmap and dropped by compact_device() once evicted clauses are a fifth
+    // of the device database.
+    int64_t budget_ = 0;
+    int64_t evicted_ = 0;
+    int64_t n_dead_ = 0;     // tombstones in meta_
+    int64_t dev_dead_ = 0;   // evicted clauses still in the device arrays
+    size_t evict_cursor_ = 0;
+    int32_t pass_no_ = 0;
+    std::vector<uint32_t> h_alive_;  // bit per meta_ index
+    DevBuf d_alive_;
+    bool alive_synced_ = false;      // d_alive_ holds h_alive_ except [alive_lo_, alive_hi_)
+    size_t alive_lo_ = SIZE_MAX, alive_hi_ = 0;
+    int64_t device_compactions_ = 0;
 
     // assignments
     int n_vars_ = 0;

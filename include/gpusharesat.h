@@ -279,7 +279,55 @@ int64_t gss_sharer_one_solver_stat(gss_sharer *s, int solver, int stat);     /* 
 /* Extensions without a counterpart in GpuClauseSharer: raise the longest
  * accepted clause (up to gss_max_clause_len()), pick the check kernel. */
 int gss_sharer_set_max_clause_len(gss_sharer *s, int n);
+/* HBM budget for the serving loop: when a pass would check more than
+ * max_clauses live clauses, the oldest clauses not reported in the last 8
+ * passes are evicted first (then the oldest of the rest); 0 = no budget. */
+int gss_sharer_set_clause_budget(gss_sharer *s, int64_t max_clauses);
+int64_t gss_sharer_evicted_count(gss_sharer *s);
+/* Order-preserving compactions of the device database that dropped evicted
+ * clauses on the GPU. */
+int64_t gss_sharer_device_compactions(gss_sharer *s);
 int gss_sharer_set_variant(gss_sharer *s, int kind, int lanes_per_clause, int depth, int flags);
+
+/* ---- serving load generator (no counterpart in the reference) ----
+ * Simulated solver threads drive one sharer on the calling thread's current
+ * device the way GpuHelpedSolver does (glucose-syrup/gpu/GpuHelpedSolver.cc:
+ * 109-157): trail-like assignments arriving in Poisson batches, a GPU thread
+ * running gpu_run in a loop, and a stream of new clauses against an HBM
+ * clause budget. Latency of an assignment = from its arrival until
+ * last_assig_all_reported passes it. */
+typedef struct gss_serving_params {
+    double seconds;            /* measured time */
+    double warmup_seconds;
+    double assign_rate;        /* aggregate assignments per second */
+    int n_solvers;
+    int n_vars;
+    int64_t budget;            /* HBM budget in clauses (0: none) */
+    int64_t initial_clauses;   /* database at the start */
+    double clause_rate;        /* stream of new clauses per second */
+    double plant_rate;         /* fraction of stream clauses planted to report */
+    int batch_max;             /* batches of 1..batch_max assignments */
+    double trail_fraction;     /* initial trail length / n_vars */
+    int trail_change;          /* an assignment unsets and sets 1..trail_change literals */
+    uint64_t seed;
+} gss_serving_params;
+
+typedef struct gss_serving_result {
+    double p50_ms, p99_ms, p999_ms, mean_ms, max_ms;
+    int64_t assignments;       /* completed in the measured window */
+    int64_t reports_popped;
+    int64_t passes;
+    double checks_per_s;       /* clause x assignment checks per second, measured window */
+    double assignments_per_s;
+    double elapsed_s;
+    int64_t evicted;
+    int64_t retries;           /* submissions that found the solver's slots full */
+    int64_t clauses_streamed;
+    int64_t live_clauses_end;
+    int64_t device_compactions;
+} gss_serving_result;
+
+int gss_serving_run(const gss_serving_params *p, gss_serving_result *res);
 
 /* ---- the reduceDb policy on its own (host only, no GPU needed) ----
  * Clause activity with decay, bump and rescale, and the thresholds a reduceDb
