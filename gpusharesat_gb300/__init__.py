@@ -90,6 +90,26 @@ def load():
     _sig(lib, "gss_check_copy_reports", c_int, vp, vp, c_i64, vp)
     _sig(lib, "gss_check_pass_host", c_int, vp, vp, c_i64, c_int, vp, vp, vp, c_i64, vp)
     _sig(lib, "gss_check_passes_host", c_int, vp, c_int, vp, c_i64, c_int, vp, vp, vp, vp, vp)
+    _sig(lib, "gss_db_positions", c_int, vp, vp, c_i64, vp)
+    _sig(lib, "gss_order_params_default", None, vp)
+    _sig(lib, "gss_order_enable", c_int, vp, vp)
+    _sig(lib, "gss_order_disable", c_int, vp)
+    _sig(lib, "gss_order_set_active", c_int, vp, c_int)
+    _sig(lib, "gss_db_set_lbd", c_int, vp, vp, vp, c_i64)
+    _sig(lib, "gss_check_wait_head", c_int, vp, vp, c_i64, vp)
+    _sig(lib, "gss_order_get_stats", c_int, vp, vp)
+    _sig(lib, "gss_order_train", c_int, vp)
+    _sig(lib, "gss_order_clause_features", c_int, vp, vp, c_i64, vp)
+    _sig(lib, "gss_order_get_weights", c_int, vp, vp)
+    _sig(lib, "gss_order_set_weights", c_int, vp, vp)
+    _sig(lib, "gss_scorer_create", c_int, c_int, ctypes.c_uint64, vp)
+    _sig(lib, "gss_scorer_destroy", c_int, vp)
+    _sig(lib, "gss_scorer_get_weights", c_int, vp, vp)
+    _sig(lib, "gss_scorer_set_weights", c_int, vp, vp)
+    _sig(lib, "gss_scorer_infer", c_int, vp, vp, c_i64, vp)
+    _sig(lib, "gss_scorer_gradient", c_int, vp, vp, vp, c_i64, vp, vp)
+    _sig(lib, "gss_scorer_train_step", c_int, vp, vp, vp, c_i64, ctypes.c_float, vp)
+    _sig(lib, "gss_bench_plant", c_int, vp, vp, c_i64, vp, vp, vp, c_i64, c_int, ctypes.c_uint64, c_i64, c_int, vp)
     _lib = lib
     return lib
 
@@ -212,6 +232,16 @@ class Engine:
         _check(rc)
         return int(n.value)
 
+    def reports(self):
+        """Reports of the pass just waited for (no relaunch)."""
+        n = self.wait()
+        if n < 0:
+            raise GssError(GSS_ERR_OVERFLOW, "report queues overflowed")
+        out = np.zeros(max(n, 1), dtype=REPORT_DTYPE)
+        got = ctypes.c_int64()
+        _check(self.lib.gss_check_copy_reports(self.h, _ptr(out), out.shape[0], ctypes.byref(got)))
+        return out[:got.value]
+
     def check(self):
         """Runs one pass (re-running after an overflow) and returns the reports."""
         for _ in range(4):
@@ -223,6 +253,72 @@ class Engine:
                 _check(self.lib.gss_check_copy_reports(self.h, _ptr(out), out.shape[0], ctypes.byref(got)))
                 return out[:got.value]
         raise GssError(GSS_ERR_OVERFLOW, "report queues kept overflowing")
+
+    def positions(self, ids):
+        """Position of each clause id in the plain scan order (-1: absent)."""
+        ids = np.ascontiguousarray(ids, dtype=np.uint32)
+        out = np.zeros(ids.shape[0], dtype=np.int64)
+        _check(self.lib.gss_db_positions(self.h, _ptr(ids), ids.shape[0], _ptr(out)))
+        return out
+
+    # ---- learned scan order ----
+
+    def order_enable(self, **params):
+        """Enables the learned scan order; params: fields of OrderParams."""
+        p = OrderParams()
+        self.lib.gss_order_params_default(ctypes.byref(p))
+        for k, v in params.items():
+            if not hasattr(p, k):
+                raise KeyError(k)
+            setattr(p, k, v)
+        _check(self.lib.gss_order_enable(self.h, ctypes.byref(p)))
+
+    def order_disable(self):
+        _check(self.lib.gss_order_disable(self.h))
+
+    def order_set_active(self, on=True):
+        _check(self.lib.gss_order_set_active(self.h, 1 if on else 0))
+
+    def set_lbd(self, ids, lbd):
+        ids = np.ascontiguousarray(ids, dtype=np.uint32)
+        lbd = np.ascontiguousarray(lbd, dtype=np.uint16)
+        _check(self.lib.gss_db_set_lbd(self.h, _ptr(ids), _ptr(lbd), ids.shape[0]))
+
+    def wait_head(self, cap=1 << 20):
+        """Reports of the head of the ordered pass in flight."""
+        while True:
+            out = np.zeros(max(int(cap), 1), dtype=REPORT_DTYPE)
+            n = ctypes.c_int64()
+            rc = self.lib.gss_check_wait_head(self.h, _ptr(out), out.shape[0], ctypes.byref(n))
+            if rc == GSS_ERR_OVERFLOW and n.value > out.shape[0]:
+                cap = int(n.value)
+                continue
+            _check(rc)
+            return out[:n.value]
+
+    def order_stats(self):
+        st = OrderStats()
+        _check(self.lib.gss_order_get_stats(self.h, ctypes.byref(st)))
+        return {name: getattr(st, name) for name, _ in OrderStats._fields_}
+
+    def order_train(self):
+        _check(self.lib.gss_order_train(self.h))
+
+    def order_features(self, ids):
+        ids = np.ascontiguousarray(ids, dtype=np.uint32)
+        x = np.zeros((ids.shape[0], SCORER_FEATURES), dtype=np.float32)
+        _check(self.lib.gss_order_clause_features(self.h, _ptr(ids), ids.shape[0], _ptr(x)))
+        return x
+
+    def order_weights(self):
+        w = np.zeros(SCORER_PARAMS, dtype=np.float32)
+        _check(self.lib.gss_order_get_weights(self.h, _ptr(w)))
+        return w
+
+    def set_order_weights(self, w):
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        assert w.shape == (SCORER_PARAMS,)
+        _check(self.lib.gss_order_set_weights(self.h, _ptr(w)))
 
     def pass_host(self, state, start, solver_of_word=None, out=None):
         """One pass through host buffers (state H2D, check, reports D2H)."""
@@ -240,6 +336,89 @@ class Engine:
                 continue
             _check(rc)
             return out[:n.value]
+
+
+SCORER_FEATURES = 12
+SCORER_HIDDEN = 64
+SCORER_PARAMS = 5057
+
+
+class OrderParams(ctypes.Structure):
+    """gss_order_params."""
+    _fields_ = [("head_fraction", ctypes.c_double), ("retrain_interval", ctypes.c_int), ("train_epochs", ctypes.c_int),
+                ("batch", ctypes.c_int), ("learning_rate", ctypes.c_float), ("log_capacity", ctypes.c_int64),
+                ("log_rate", ctypes.c_double), ("seed", ctypes.c_uint64)]
+
+
+class OrderStats(ctypes.Structure):
+    """gss_order_stats."""
+    _fields_ = [("passes", ctypes.c_int64), ("trainings", ctypes.c_int64), ("last_loss", ctypes.c_double),
+                ("head_positions", ctypes.c_int64), ("logged", ctypes.c_int64), ("score_ms", ctypes.c_double),
+                ("head_ms", ctypes.c_double), ("tail_ms", ctypes.c_double)]
+
+
+class Scorer:
+    """The learned order's MLP (12-64-64-1) on its own: FP32 weights, BF16
+    tensor-core inference, FP32 training kernels. Flat weight layout:
+    W1[64][12], b1[64], W2[64][64], b2[64], w3[64], b3."""
+
+    def __init__(self, device=0, seed=1):
+        self.lib = load()
+        h = ctypes.c_void_p()
+        _check(self.lib.gss_scorer_create(device, seed, ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.gss_scorer_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def weights(self):
+        w = np.zeros(SCORER_PARAMS, dtype=np.float32)
+        _check(self.lib.gss_scorer_get_weights(self.h, _ptr(w)))
+        return w
+
+    def set_weights(self, w):
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        assert w.shape == (SCORER_PARAMS,)
+        _check(self.lib.gss_scorer_set_weights(self.h, _ptr(w)))
+
+    def infer(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, SCORER_FEATURES)
+        out = np.zeros(x.shape[0], dtype=np.float32)
+        _check(self.lib.gss_scorer_infer(self.h, _ptr(x), x.shape[0], _ptr(out)))
+        return out
+
+    def gradient(self, x, y):
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, SCORER_FEATURES)
+        y = np.ascontiguousarray(y, dtype=np.float32)
+        g = np.zeros(SCORER_PARAMS, dtype=np.float32)
+        loss = ctypes.c_float()
+        _check(self.lib.gss_scorer_gradient(self.h, _ptr(x), _ptr(y), x.shape[0], _ptr(g), ctypes.byref(loss)))
+        return g, float(loss.value)
+
+    def train_step(self, x, y, lr=1e-3):
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, SCORER_FEATURES)
+        y = np.ascontiguousarray(y, dtype=np.float32)
+        loss = ctypes.c_float()
+        _check(self.lib.gss_scorer_train_step(self.h, _ptr(x), _ptr(y), x.shape[0], ctypes.c_float(lr),
+                                              ctypes.byref(loss)))
+        return float(loss.value)
+
+
+def bench_plant(lits_ptr, offsets_ptr, n_clauses, rate_ptr, state_ptr, base_ptr, n_vars, n_words, seed, pass_no,
+                restore, stream=None):
+    """gss_bench_plant on device pointers (the learned-order workload)."""
+    lib = load()
+    _check(lib.gss_bench_plant(_vp(lits_ptr), _vp(offsets_ptr), int(n_clauses), _vp(rate_ptr), _vp(state_ptr),
+                               _vp(base_ptr), int(n_vars), int(n_words), int(seed), int(pass_no), int(restore),
+                               _vp(stream) if stream else None))
 
 
 def passes_host(engine, states, start, solver_of_word=None, caps=None):

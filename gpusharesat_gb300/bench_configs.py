@@ -6,6 +6,7 @@ baseline, and prints one JSON line per pass plus a summary line:
 
     python -m gpusharesat_gb300.bench_configs batching [--clauses 8000000 --passes 6]
     python -m gpusharesat_gb300.bench_configs serving [--rates 5e4 1e5 2e5 --budget 16000000]
+    python -m gpusharesat_gb300.bench_configs learned [--clauses 4000000 --passes 3000 --retrain 1000]
 
 batching: 8e6 clauses (lengths 1 + Zipf(1.2), at most 256), 48 solvers sending
     uneven batches of 4..64 assignments per pass (two 32-slot words each), 5%
@@ -25,6 +26,17 @@ serving: 2^21 variables; 64 solver threads with trails of half the variables
     report) flows into an HBM budget of 16e6 clauses, full from the start.
     Reports p50/p99/p999 latency from an assignment's arrival to the moment
     every report of it is delivered, and sustained checks/s.
+
+learned: 2^21 variables; 4e6 clauses at the start (lengths 1 + Zipf(1.2),
+    at most 256) plus a stream of 500 new clauses per pass (as many of the
+    oldest deleted), 64 words x 32 slots per pass. Clauses are built over a
+    hidden model and the slots agree with it, so a clause reports only when
+    planted; clause c is planted in a pass with latent probability
+    r_c ~ Beta(0.5, 20), and its LBD falls with r_c. The order retrains every
+    1000 passes. Reports the share of report bits delivered with the first
+    10% of the scan, against the plain order's first 10%, the delivery
+    latency of report bits (from the launch call to the moment the host has
+    them), and that each compared pass reports what the plain scan reports.
 """
 import argparse
 import json
@@ -169,21 +181,166 @@ def serving(args):
     return summary
 
 
+def _bits(rep):
+    """Report bits (clause x slot pairs) of a report array."""
+    return int(np.unpackbits(np.ascontiguousarray(rep["mask"]).view(np.uint8)).sum()) if len(rep) else 0
+
+
+def _weighted_quantile(values, weights, q):
+    order = np.argsort(values)
+    v, w = np.asarray(values)[order], np.asarray(weights, dtype=np.float64)[order]
+    c = np.cumsum(w)
+    if c[-1] <= 0:
+        return 0.0
+    return float(v[np.searchsorted(c, q * c[-1])])
+
+
+def learned(args):
+    """Learned scan order against the plain scan on one stream of passes.
+
+    Per pass: plant reports at the clauses' latent rates into the base state
+    (device), then the ordered pass (scoring, head launch, tail launch) with
+    its head delivered early, and, every compare_every passes, the plain
+    single-launch pass over the same state, whose report set must equal the
+    ordered pass's. The stream appends stream_per_pass new clauses and
+    deletes as many of the oldest before each pass."""
+    import torch
+    t0 = time.time()
+    P, k = args.passes, args.stream_per_pass
+    d = W.make_learned(seed=4, n_vars=2 ** 21, n_clauses=args.clauses, n_words=64, stream=k * P)
+    n0, n_vars, n_words = d["n_clauses"], d["n_vars"], d["n_words"]
+    lits, offsets = d["lits"], d["offsets"]
+    print(json.dumps({"config": "learned", "clauses": n0, "stream_per_pass": k, "passes": P,
+                      "literals": int(offsets[n0]), "vars": n_vars, "slots": 32 * n_words,
+                      "setup_s": round(time.time() - t0, 1)}), flush=True)
+    dev = torch.device("cuda:0")
+    d_lits = torch.from_numpy(lits).to(dev)
+    d_off = torch.from_numpy(offsets).to(dev)
+    rate_all = torch.from_numpy(d["rate"]).to(dev)
+    d_rate = torch.zeros_like(rate_all)
+    d_rate[:n0] = rate_all[:n0]
+    base = torch.from_numpy(d["state"].view(np.int32)).to(dev)
+    state = base.clone()
+    start = torch.full((n_words,), -1, dtype=torch.int32, device=dev)
+    eng = g.Engine(0)
+    eng.set_db(lits[:offsets[n0]], offsets[:n0 + 1])
+    eng.order_enable(head_fraction=args.head_fraction, retrain_interval=args.retrain, train_epochs=2, seed=4)
+    eng.set_lbd(np.arange(n0, dtype=np.uint32), d["lbd"][:n0])
+    eng.set_capacity(1 << 22)
+    lo, nxt = 0, n0
+    rows = []
+    for p in range(P):
+        if p > 0 and k:
+            ids = np.arange(nxt, nxt + k, dtype=np.uint32)
+            b0, b1 = int(offsets[nxt]), int(offsets[nxt + k])
+            eng.append_db(lits[b0:b1], offsets[nxt:nxt + k + 1] - b0, ids)
+            eng.set_lbd(ids, d["lbd"][nxt:nxt + k])
+            eng.delete(np.arange(lo, lo + k, dtype=np.uint32))
+            d_rate[nxt:nxt + k] = rate_all[nxt:nxt + k]
+            d_rate[lo:lo + k] = 0
+            nxt += k
+            lo += k
+        g.bench_plant(d_lits.data_ptr(), d_off.data_ptr(), nxt, d_rate.data_ptr(), state.data_ptr(),
+                      base.data_ptr(), n_vars, n_words, 4, p, 0)
+        torch.cuda.synchronize()
+        eng.set_state_device(state.data_ptr(), n_vars, n_words, start.data_ptr())
+        eng.wait()
+        ta = time.perf_counter()
+        eng.launch()
+        head = eng.wait_head()
+        tb = time.perf_counter()
+        full = eng.reports()
+        tc = time.perf_counter()
+        st = eng.order_stats()
+        row = {"pass": p, "head_bits": _bits(head), "bits": _bits(full), "head_ms": (tb - ta) * 1e3,
+               "all_ms": (tc - ta) * 1e3, "score_dev_ms": st["score_ms"], "head_dev_ms": st["head_ms"],
+               "tail_dev_ms": st["tail_ms"], "trainings": st["trainings"]}
+        if p % args.compare_every == 0:
+            eng.order_set_active(False)
+            eng.set_timing(True)
+            eng.kernel_time()
+            td = time.perf_counter()
+            eng.launch()
+            plain = eng.reports()
+            te = time.perf_counter()
+            row["plain_all_ms"] = (te - td) * 1e3
+            row["plain_dev_ms"] = eng.kernel_time()[0]
+            eng.set_timing(False)
+            eng.order_set_active(True)
+            def key(r):
+                o = np.lexsort((r["mask"], r["word"], r["clause"]))
+                return np.stack([r["clause"][o], r["word"][o], r["mask"][o]])
+            row["same_reports"] = bool(len(plain) == len(full) and np.array_equal(key(plain), key(full)))
+            # share of report bits in the first head_fraction of the plain order
+            pos = eng.positions(plain["clause"])
+            first = pos < int(np.ceil(args.head_fraction * eng.clause_count))
+            row["plain_head_bits"] = _bits(plain[first])
+        rows.append(row)
+        g.bench_plant(d_lits.data_ptr(), d_off.data_ptr(), nxt, d_rate.data_ptr(), state.data_ptr(),
+                      base.data_ptr(), n_vars, n_words, 4, p, 1)
+        torch.cuda.synchronize()
+        if p % 100 == 0:
+            print(json.dumps(row), flush=True)
+    trained = [r for r in rows if r["trainings"] >= 1 and r["bits"]]
+    cmp_rows = [r for r in trained if "plain_all_ms" in r]
+    recall = float(np.sum([r["head_bits"] for r in trained]) / max(1, np.sum([r["bits"] for r in trained])))
+    plain_recall = float(np.sum([r["plain_head_bits"] for r in cmp_rows]) /
+                         max(1, np.sum([r["bits"] for r in cmp_rows])))
+    # delivery latency of each report bit, from the pass's launch call
+    lv, lw, pv, pw = [], [], [], []
+    for r in cmp_rows:
+        lv += [r["head_ms"], r["all_ms"]]
+        lw += [r["head_bits"], r["bits"] - r["head_bits"]]
+        pv.append(r["plain_all_ms"])
+        pw.append(r["bits"])
+    checks_ordered = [(nxt - lo) * 32 * n_words / (r["all_ms"] / 1e3) for r in cmp_rows]
+    checks_plain = [(nxt - lo) * 32 * n_words / (r["plain_all_ms"] / 1e3) for r in cmp_rows]
+    summary = {"config": "learned", "passes": P, "trained_passes": len(trained), "compared_passes": len(cmp_rows),
+               "head_fraction": args.head_fraction,
+               "recall_first_10pct_learned": recall, "recall_first_10pct_plain": plain_recall,
+               "latency_mean_ms_learned": float(np.average(lv, weights=lw)) if cmp_rows else None,
+               "latency_mean_ms_plain": float(np.average(pv, weights=pw)) if cmp_rows else None,
+               "latency_p50_ms_learned": _weighted_quantile(lv, lw, 0.5) if cmp_rows else None,
+               "latency_p50_ms_plain": _weighted_quantile(pv, pw, 0.5) if cmp_rows else None,
+               "latency_p99_ms_learned": _weighted_quantile(lv, lw, 0.99) if cmp_rows else None,
+               "latency_p99_ms_plain": _weighted_quantile(pv, pw, 0.99) if cmp_rows else None,
+               "pass_ms_learned": float(np.mean([r["all_ms"] for r in cmp_rows])) if cmp_rows else None,
+               "pass_ms_plain": float(np.mean([r["plain_all_ms"] for r in cmp_rows])) if cmp_rows else None,
+               "score_dev_ms": float(np.mean([r["score_dev_ms"] for r in trained])) if trained else None,
+               "checks_per_s_learned": float(np.mean(checks_ordered)) if cmp_rows else None,
+               "checks_per_s_plain": float(np.mean(checks_plain)) if cmp_rows else None,
+               "same_reports_every_compared_pass": all(r["same_reports"] for r in rows if "same_reports" in r),
+               "trainings": rows[-1]["trainings"] if rows else 0}
+    print(json.dumps(summary), flush=True)
+    eng.close()
+    return summary
+
+
 def main(argv=None):
     p = argparse.ArgumentParser()
-    p.add_argument("config", choices=["batching", "serving"])
+    p.add_argument("config", choices=["batching", "serving", "learned"])
     p.add_argument("--clauses", type=int, default=8_000_000)
     p.add_argument("--passes", type=int, default=6)
     p.add_argument("--rates", type=float, nargs="+", default=[5e4, 1e5, 2e5])
     p.add_argument("--budget", type=int, default=16_000_000)
     p.add_argument("--seconds", type=float, default=10.0)
     p.add_argument("--warmup-seconds", type=float, default=2.0)
+    p.add_argument("--stream-per-pass", type=int, default=500)
+    p.add_argument("--retrain", type=int, default=1000)
+    p.add_argument("--head-fraction", type=float, default=0.1)
+    p.add_argument("--compare-every", type=int, default=5)
     args = p.parse_args(argv)
+    if args.config == "learned" and "--clauses" not in (argv or sys.argv):
+        args.clauses = 4_000_000
+    if args.config == "learned" and "--passes" not in (argv or sys.argv):
+        args.passes = 3000
     build.build()
     if args.config == "batching":
         batching(args)
     elif args.config == "serving":
         serving(args)
+    elif args.config == "learned":
+        learned(args)
 
 
 if __name__ == "__main__":

@@ -124,14 +124,16 @@ __global__ void __launch_bounds__(kWarps * 32) check_kernel(CheckArgs a) {
     const uint64_t pol_keep = policy_evict_last();
     const uint64_t pol_stream = policy_evict_first();
 
-    const uint32_t n_groups = (a.n_clauses + CPW - 1) / CPW;
+    const uint32_t n_scan = scan_count(a);
+    const uint32_t n_groups = (n_scan + CPW - 1) / CPW;
     const uint64_t n_tasks = (uint64_t) n_groups * a.n_blocks;
     const uint64_t stride = (uint64_t) gridDim.x * kWarps;
     for (uint64_t task = (uint64_t) blockIdx.x * kWarps + wib; task < n_tasks; task += stride) {
         // Slot block outermost: all warps sweep block 0 first, then block 1...
         const uint32_t blk = (uint32_t) (task / n_groups);
         const uint32_t g = (uint32_t) (task - (uint64_t) blk * n_groups);
-        const uint32_t c = g * CPW + grp;
+        const uint32_t i = g * CPW + grp;
+        const uint32_t c = i < n_scan ? scan_clause(a, i) : 0xFFFFFFFFu;
         const bool valid = c < a.n_clauses && clause_live(a, c);
         const uint32_t w = blk * LPC + sub;
         uint32_t all_false = valid ? __ldg(a.start + w) : 0u;  // start is padded to n_blocks*LPC
@@ -256,13 +258,15 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) check_wide_kernel(CheckArgs
     uint32_t *counter = a.counts + part;
     uint32_t nstaged = 0;
 
-    const uint32_t n_groups = (a.n_clauses + CPW - 1) / CPW;
+    const uint32_t n_scan = scan_count(a);
+    const uint32_t n_groups = (n_scan + CPW - 1) / CPW;
     const uint64_t n_tasks = (uint64_t) n_groups * a.n_blocks;
     const uint64_t stride = (uint64_t) gridDim.x * kWarps;
     for (uint64_t task = (uint64_t) blockIdx.x * kWarps + wib; task < n_tasks; task += stride) {
         const uint32_t blk = (uint32_t) (task / n_groups);
         const uint32_t g = (uint32_t) (task - (uint64_t) blk * n_groups);
-        const uint32_t c = g * CPW + grp;
+        const uint32_t i = g * CPW + grp;
+        const uint32_t c = i < n_scan ? scan_clause(a, i) : 0xFFFFFFFFu;
         const bool valid = c < a.n_clauses && clause_live(a, c);
         const uint32_t w0 = blk * BW + sub * WPL;
         uint32_t af[WPL], ou[WPL];
@@ -364,7 +368,8 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) check_wide_pf_kernel(CheckA
     uint32_t *counter = a.counts + part;
     uint32_t nstaged = 0;
 
-    const uint32_t n_groups = (a.n_clauses + CPW - 1) / CPW;
+    const uint32_t n_scan = scan_count(a);
+    const uint32_t n_groups = (n_scan + CPW - 1) / CPW;
     const uint64_t n_tasks = (uint64_t) n_groups * a.n_blocks;
     const uint64_t stride = (uint64_t) gridDim.x * kWarps;
     uint64_t task = (uint64_t) blockIdx.x * kWarps + wib;
@@ -372,7 +377,8 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) check_wide_pf_kernel(CheckA
     // clause of this lane's group for a task
     auto clause_of = [&](uint64_t t) -> uint32_t {
         const uint32_t b = (uint32_t) (t / n_groups);
-        return (uint32_t) (t - (uint64_t) b * n_groups) * CPW + grp;
+        const uint32_t i = (uint32_t) (t - (uint64_t) b * n_groups) * CPW + grp;
+        return i < n_scan ? scan_clause(a, i) : 0xFFFFFFFFu;
     };
     // prefetched: offsets and first literal chunk of the current task
     uint32_t nx_pos = 0, nx_end = 0;
@@ -505,7 +511,8 @@ __global__ void __launch_bounds__(kWarps * 32, 1) check_wide_persist_kernel(cons
     uint32_t *counter = a.counts + part;
     uint32_t nstaged = 0;
 
-    const uint32_t n_groups = (a.n_clauses + CPW - 1) / CPW;
+    const uint32_t n_scan = scan_count(a);
+    const uint32_t n_groups = (n_scan + CPW - 1) / CPW;
     const uint64_t n_tasks = (uint64_t) n_groups * a.n_blocks;
     while (true) {
         uint32_t first = 0;
@@ -516,7 +523,8 @@ __global__ void __launch_bounds__(kWarps * 32, 1) check_wide_persist_kernel(cons
         for (uint64_t task = first; task < last; task++) {
             const uint32_t blk = (uint32_t) (task / n_groups);
             const uint32_t g = (uint32_t) (task - (uint64_t) blk * n_groups);
-            const uint32_t c = g * CPW + grp;
+            const uint32_t i = g * CPW + grp;
+            const uint32_t c = i < n_scan ? scan_clause(a, i) : 0xFFFFFFFFu;
             const bool valid = c < a.n_clauses && clause_live(a, c);
             const uint32_t w0 = blk * BW + sub * WPL;
             uint32_t af[WPL], ou[WPL];
@@ -613,7 +621,7 @@ int launch_wide_pf_variant(const CheckArgs &a, cudaStream_t stream, int sm_count
                                                                kWarps * 32, 0));
     if (per_sm < 1) per_sm = 1;
     constexpr int CPW = 32 / LPC;
-    const uint64_t n_tasks = (uint64_t) ((a.n_clauses + CPW - 1) / CPW) * a.n_blocks;
+    const uint64_t n_tasks = (uint64_t) ((scan_count(a) + CPW - 1) / CPW) * a.n_blocks;
     uint64_t blocks = (uint64_t) sm_count * per_sm;
     const uint64_t need = (n_tasks + kWarps - 1) / kWarps;
     if (blocks > need) blocks = need;
@@ -630,7 +638,7 @@ int launch_wide_variant(const CheckArgs &a, cudaStream_t stream, int sm_count) {
                                                                kWarps * 32, 0));
     if (per_sm < 1) per_sm = 1;
     constexpr int CPW = 32 / LPC;
-    const uint64_t n_tasks = (uint64_t) ((a.n_clauses + CPW - 1) / CPW) * a.n_blocks;
+    const uint64_t n_tasks = (uint64_t) ((scan_count(a) + CPW - 1) / CPW) * a.n_blocks;
     uint64_t blocks = (uint64_t) sm_count * per_sm;
     const uint64_t need = (n_tasks + kWarps - 1) / kWarps;
     if (blocks > need) blocks = need;
@@ -662,7 +670,7 @@ int launch_variant(const CheckArgs &a, cudaStream_t stream, int sm_count) {
     GSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, check_kernel<LPC, G>, kWarps * 32, 0));
     if (per_sm < 1) per_sm = 1;
     constexpr int CPW = 32 / LPC;
-    const uint64_t n_tasks = (uint64_t) ((a.n_clauses + CPW - 1) / CPW) * a.n_blocks;
+    const uint64_t n_tasks = (uint64_t) ((scan_count(a) + CPW - 1) / CPW) * a.n_blocks;
     uint64_t blocks = (uint64_t) sm_count * per_sm;
     const uint64_t need = (n_tasks + kWarps - 1) / kWarps;
     if (blocks > need) blocks = need;
@@ -687,7 +695,7 @@ bool valid_wide_variant(int wpl, int lpc, int g, int occ) {
 }
 
 int launch_check_wide_pf(const CheckArgs &a, int wpl, int occ, cudaStream_t stream, int sm_count) {
-    if (a.n_clauses == 0 || a.n_blocks == 0) return GSS_OK;
+    if (a.n_clauses == 0 || a.n_blocks == 0 || scan_count(a) == 0) return GSS_OK;
 #define GSS_PV(W, L, GG)                                                                      \
     if (wpl == W && a.lpc == L && a.g == GG)                                                  \
         return occ ? launch_wide_pf_variant<W, L, GG, 4>(a, stream, sm_count)                 \
@@ -727,7 +735,7 @@ bool valid_wide_pf_variant(int wpl, int lpc, int g) {
 }
 
 int launch_check_wide(const CheckArgs &a, int wpl, int occ, cudaStream_t stream, int sm_count) {
-    if (a.n_clauses == 0 || a.n_blocks == 0) return GSS_OK;
+    if (a.n_clauses == 0 || a.n_blocks == 0 || scan_count(a) == 0) return GSS_OK;
 #define GSS_WV(W, L, GG)                                                                      \
     if (wpl == W && a.lpc == L && a.g == GG)                                                  \
         return occ ? launch_wide_variant<W, L, GG, 8>(a, stream, sm_count)                    \
@@ -756,7 +764,7 @@ bool valid_variant(int lpc, int g) {
 }
 
 int launch_check(const CheckArgs &a, cudaStream_t stream, int sm_count) {
-    if (a.n_clauses == 0 || a.n_blocks == 0) return GSS_OK;
+    if (a.n_clauses == 0 || a.n_blocks == 0 || scan_count(a) == 0) return GSS_OK;
 #define GSS_VARIANT(L, GG) \
     if (a.lpc == L && a.g == GG) return launch_variant<L, GG>(a, stream, sm_count);
     GSS_VARIANT(1, 1)
@@ -855,6 +863,8 @@ extern "C" int gss_check_noalloc(const int32_t *lits, const int64_t *offsets, ui
         a.offsets = offsets;
         a.orig = nullptr;
         a.n_clauses = n_clauses;
+        a.scan_begin = 0;
+        a.scan_end = n_clauses;
         a.state = (const uint2 *) state;
         a.n_vars = n_vars;
         a.n_blocks = n_blocks;

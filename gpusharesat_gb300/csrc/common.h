@@ -89,7 +89,19 @@ struct CheckArgs {
     uint32_t *err;                // device flag, set to nonzero when a bounded wait gives up
     const uint32_t *alive;        // device, 1 bit per clause (NULL: every clause is live)
     uint32_t alive_by_id;         // alive is indexed by orig[c] rather than by c
+    // Scan order: this launch checks the clauses at scan positions
+    // [scan_begin, scan_end); position i is clause perm[i] (NULL: clause i).
+    const uint32_t *perm;
+    uint32_t scan_begin, scan_end;
 };
+
+__host__ __device__ __forceinline__ uint32_t scan_count(const CheckArgs &a) {
+    return a.scan_end > a.scan_begin ? a.scan_end - a.scan_begin : 0u;
+}
+// Clause at offset i of this launch's scan range (i < scan_count).
+__device__ __forceinline__ uint32_t scan_clause(const CheckArgs &a, uint32_t i) {
+    return a.perm ? __ldg(a.perm + a.scan_begin + i) : a.scan_begin + i;
+}
 
 // Whether clause c of the database takes part in the pass.
 __device__ __forceinline__ bool clause_live(const CheckArgs &a, uint32_t c) {

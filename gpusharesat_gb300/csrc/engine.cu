@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "common.h"
+#include "engine.h"
 
 namespace gss {
 
@@ -90,81 +91,6 @@ void PinnedBuf::release() {
 
 using namespace gss;
 
-struct gss_engine {
-    int device = 0;
-    int sm_count = 0;
-    cudaStream_t own_stream = nullptr;
-    cudaStream_t stream = nullptr;
-    int64_t launches = 0;
-
-    // clause database: CSR, clauses sorted by length (stable), with the
-    // original index of each sorted clause
-    DevBuf lits, offsets, orig;
-    int64_t n_clauses = 0, n_lits = 0, max_var = -1;
-    // tiles of the tiled kernel (first clause / first literal of each tile)
-    DevBuf tile_clause, tile_lit;
-    uint32_t n_tiles = 0;
-    bool tiles_stale = true;
-    // host mirror of the database, in device order, for appends, deletes and
-    // compaction; alive bits (1 per device clause) mark deleted clauses
-    std::vector<int32_t> h_lits;
-    std::vector<int64_t> h_off;
-    std::vector<uint32_t> h_ids;
-    std::vector<uint32_t> index_of;  // clause id -> device index (0xFFFFFFFF: none)
-    std::vector<uint32_t> h_alive;
-    DevBuf alive;
-    bool alive_dirty = false;
-    int64_t n_dead = 0;
-    uint32_t next_id = 0;
-
-    // kernel variant: kind (GSS_KERNEL_*), lanes (words) per clause (0 = pick
-    // from the word count), loads in flight / clause slots, cache hints
-    int kind = GSS_KERNEL_AUTO, lpc = 0, g = 2, flags = 0;
-    DevBuf err;
-
-    // assignment state, block-major [n_blocks][n_vars][state_bw words]
-    DevBuf state, state_raw, start, solver_of_word;
-    int64_t n_vars = 0;
-    int n_words = 0;
-    int n_blocks = 0;
-    // effective variant the state was laid out for (resolved from the
-    // requested one and the word count by gss_state_set)
-    int state_kind = GSS_KERNEL_DIRECT;
-    int state_lpc = 0;  // lanes per clause
-    int state_g = 2;
-    int state_bw = 0;   // words per slot block
-
-    // report queues: n_parts partitions of cap_per_part records
-    DevBuf reports, counts;
-    uint32_t n_parts = 16;
-    uint32_t cap_per_part = 0;
-    int64_t requested_cap = 0;
-    PinnedBuf h_counts;
-    bool pass_pending = false;
-
-    // pipelined passes through host buffers (gss_check_passes_host): second
-    // state and report buffers, copy streams and events
-    DevBuf state2, state_raw2, reports2, counts2;
-    PinnedBuf h_counts2;
-    cudaStream_t h2d = nullptr, d2h = nullptr;
-    cudaEvent_t ev_h2d[2] = {nullptr, nullptr}, ev_kernel[2] = {nullptr, nullptr}, ev_d2h[2] = {nullptr, nullptr};
-
-    // persistent kernel: arguments in device memory, task counter; optional
-    // CUDA graph of a pass (memsets, kernel, count readback), recaptured when
-    // a buffer it names changes
-    DevBuf d_args, work;
-    bool use_graph = false;
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t graph_exec = nullptr;
-    std::vector<uintptr_t> graph_key;
-    int64_t graph_captures = 0;
-
-    // optional CUDA-event timing of each check kernel (on the launch stream)
-    bool timing = false;
-    std::vector<cudaEvent_t> ev_pool;
-    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_pending;
-};
-
 namespace {
 
 int words_per_lane(int kind) { return kind == GSS_KERNEL_WIDE4 ? 4 : kind == GSS_KERNEL_WIDE2 ? 2 : 1; }
@@ -244,6 +170,7 @@ int gss_engine_destroy(gss_engine *eng) {
         cudaEventDestroy(p.second);
     }
     for (auto e : eng->ev_pool) cudaEventDestroy(e);
+    order_destroy(eng);
     delete eng;
     return GSS_OK;
 }
@@ -408,6 +335,7 @@ int gss_db_set(gss_engine *eng, const int32_t *lits, const int64_t *offsets, int
     eng->h_ids.clear();
     eng->index_of.clear();
     eng->next_id = 0;
+    eng->db_epoch++;
     mirror_append(eng, lits, offsets, n_clauses, nullptr);
     GSS_TRY(upload_all(eng));
     eng->max_var = max_var;
@@ -507,6 +435,16 @@ int64_t gss_db_live_count(const gss_engine *eng) { return eng ? eng->n_clauses -
 int64_t gss_db_clause_count(const gss_engine *eng) { return eng ? eng->n_clauses : -1; }
 int64_t gss_db_literal_count(const gss_engine *eng) { return eng ? eng->n_lits : -1; }
 int64_t gss_db_max_var(const gss_engine *eng) { return eng ? eng->max_var : -1; }
+
+int gss_db_positions(const gss_engine *eng, const uint32_t *ids, int64_t n, int64_t *positions) {
+    if (!eng || n < 0 || (n > 0 && (!ids || !positions))) return set_error(GSS_ERR_INVALID, "bad arguments");
+    for (int64_t i = 0; i < n; i++) {
+        const uint32_t id = ids[i];
+        const uint32_t pos = id < eng->index_of.size() ? eng->index_of[id] : 0xFFFFFFFFu;
+        positions[i] = pos == 0xFFFFFFFFu ? -1 : (int64_t) pos;
+    }
+    return GSS_OK;
+}
 
 int gss_state_set(gss_engine *eng, const uint32_t *state, int64_t n_vars, int n_words, const uint32_t *start,
                   const int32_t *solver_of_word, int on_device) {
@@ -690,6 +628,8 @@ int launch_pass_into(gss_engine *eng, const void *state, DevBuf &reports, DevBuf
     a.offsets = (const int64_t *) eng->offsets.ptr;
     a.orig = (const uint32_t *) eng->orig.ptr;
     a.n_clauses = (uint32_t) eng->n_clauses;
+    a.scan_begin = 0;
+    a.scan_end = a.n_clauses;
     a.state = (const uint2 *) state;
     a.n_vars = (uint32_t) eng->n_vars;
     a.n_blocks = (uint32_t) eng->n_blocks;
@@ -735,6 +675,12 @@ int launch_pass_into(gss_engine *eng, const void *state, DevBuf &reports, DevBuf
         }
     }
     const bool wide = eng->state_kind == GSS_KERNEL_WIDE4 || eng->state_kind == GSS_KERNEL_WIDE2;
+    const bool ordered = order_active(eng);
+    if (ordered && (eng->state_kind == GSS_KERNEL_TILED || (eng->flags & GSS_VARIANT_PERSISTENT)))
+        return set_error(GSS_ERR_STATE, "the learned scan order runs the direct and wide kernels (not the tiled or "
+                         "persistent ones)");
+    if (ordered && (&reports != &eng->reports || &counts != &eng->counts))
+        return set_error(GSS_ERR_STATE, "the learned scan order runs through gss_check_launch");
     if (wide && (eng->flags & GSS_VARIANT_PERSISTENT)) {
         // arguments through device memory, so the same graph serves every pass
         GSS_TRY(eng->d_args.reserve(sizeof(CheckArgs)));
@@ -789,16 +735,29 @@ int launch_pass_into(gss_engine *eng, const void *state, DevBuf &reports, DevBuf
     GSS_CUDA_TRY(cudaMemsetAsync(a.counts, 0, sizeof(uint32_t) * a.n_parts, eng->stream));
     GSS_CUDA_TRY(cudaMemsetAsync(a.err, 0, sizeof(uint32_t), eng->stream));
     if (ev0) GSS_CUDA_TRY(cudaEventRecord(ev0, eng->stream));
-    if (eng->state_kind == GSS_KERNEL_TILED) {
-        GSS_TRY(launch_check_tiled(a, eng->stream, eng->sm_count));
-    } else if (wide && (eng->flags & GSS_VARIANT_PIPELINED)) {
-        GSS_TRY(launch_check_wide_pf(a, words_per_lane(eng->state_kind), (eng->flags & GSS_VARIANT_OCCUPANCY) ? 1 : 0,
-                                     eng->stream, eng->sm_count));
-    } else if (wide) {
-        GSS_TRY(launch_check_wide(a, words_per_lane(eng->state_kind), (eng->flags & GSS_VARIANT_OCCUPANCY) ? 1 : 0,
-                                  eng->stream, eng->sm_count));
+    auto launch = [&](const CheckArgs &args) -> int {
+        if (eng->state_kind == GSS_KERNEL_TILED) return launch_check_tiled(args, eng->stream, eng->sm_count);
+        const int occ = (eng->flags & GSS_VARIANT_OCCUPANCY) ? 1 : 0;
+        if (wide && (eng->flags & GSS_VARIANT_PIPELINED))
+            return launch_check_wide_pf(args, words_per_lane(eng->state_kind), occ, eng->stream, eng->sm_count);
+        if (wide) return launch_check_wide(args, words_per_lane(eng->state_kind), occ, eng->stream, eng->sm_count);
+        return launch_check(args, eng->stream, eng->sm_count);
+    };
+    if (ordered) {
+        // learned order: score and sort, then the head of the scan, its
+        // counts for early delivery, the tail, and the history update
+        uint32_t head = 0;
+        GSS_TRY(order_prepare(eng, &a.perm, &head));
+        a.scan_begin = 0;
+        a.scan_end = head;
+        if (head) GSS_TRY(launch(a));
+        GSS_TRY(order_after_head(eng, counts));
+        a.scan_begin = head;
+        a.scan_end = a.n_clauses;
+        if (head < a.n_clauses) GSS_TRY(launch(a));
+        GSS_TRY(order_after_pass(eng, reports, counts));
     } else {
-        GSS_TRY(launch_check(a, eng->stream, eng->sm_count));
+        GSS_TRY(launch(a));
     }
     if (ev1) {
         GSS_CUDA_TRY(cudaEventRecord(ev1, eng->stream));
@@ -819,6 +778,10 @@ int gss_check_wait(gss_engine *eng, int64_t *n_reports) {
     GSS_TRY(ensure_device(eng));
     GSS_CUDA_TRY(cudaStreamSynchronize(eng->stream));
     eng->pass_pending = false;
+    if (!eng->h_counts.ptr) {  // no pass launched yet: nothing to report
+        if (n_reports) *n_reports = 0;
+        return GSS_OK;
+    }
     const uint32_t *hc = (const uint32_t *) eng->h_counts.ptr;
     int64_t total = 0;
     bool overflow = false;
@@ -846,6 +809,7 @@ int gss_check_copy_reports(gss_engine *eng, gss_report *out, int64_t cap, int64_
     if (n_reports) *n_reports = total;
     if (total > cap) return set_error(GSS_ERR_OVERFLOW, "output holds %lld records, pass has %lld", (long long) cap,
                                       (long long) total);
+    if (total == 0) return GSS_OK;
     const uint32_t *hc = (const uint32_t *) eng->h_counts.ptr;
     int64_t pos = 0;
     for (uint32_t p = 0; p < eng->n_parts; p++) {

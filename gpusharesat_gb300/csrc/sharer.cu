@@ -767,6 +767,8 @@ int Sharer::run_check(Pass &p) {
     a.offsets = (const int64_t *) d_offsets_.ptr;
     a.orig = (const uint32_t *) d_orig_.ptr;
     a.n_clauses = p.n_clauses;
+    a.scan_begin = 0;
+    a.scan_end = p.n_clauses;
     a.state = (const uint2 *) d_state_.ptr;
     a.n_vars = (uint32_t) std::max(dev_vars_, 1);
     a.n_blocks = (uint32_t) n_blocks_;

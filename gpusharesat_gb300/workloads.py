@@ -257,3 +257,52 @@ def churn_batch(rng, n_vars, n_new):
     """New clauses of a churn step, from the small workload's generator
     (lengths 2..30, geometric mean 8)."""
     return distinct_var_clauses(rng, lengths_small(rng, n_new), n_vars)
+
+
+def model_clauses(rng, lengths, n_vars, model):
+    """Clauses over a hidden total assignment `model` (uint8 per variable,
+    1 = true): distinct variables, at least two literals true under the
+    model, each other literal false under it with probability 1/2. Under an
+    assignment that agrees with the model such a clause has a true or two
+    unassigned literals, so it never reports unless planted."""
+    lits, offsets = distinct_var_clauses(rng, lengths, n_vars)
+    var = lits.astype(np.int64) >> 1
+    m_true = rng.random(var.shape[0]) < 0.5
+    lengths = np.diff(offsets)
+    # two forced model-true literals per clause, at distinct random positions
+    p0 = (rng.random(lengths.shape[0]) * lengths).astype(np.int64)
+    p1 = (p0 + 1 + (rng.random(lengths.shape[0]) * (lengths - 1)).astype(np.int64)) % np.maximum(lengths, 1)
+    m_true[offsets[:-1] + p0] = True
+    m_true[offsets[:-1] + p1] = True
+    true_sign = 1 - model[var].astype(np.int64)  # sign of the model-true literal
+    sign = np.where(m_true, true_sign, 1 - true_sign)
+    return (2 * var + sign).astype(np.int32), offsets
+
+
+def make_learned(seed=4, n_vars=2 ** 21, n_clauses=4_000_000, n_words=64, stream=0, assigned=0.5):
+    """Learned scan order: a pool of n_clauses + stream clauses (the first
+    n_clauses are the database at the start, the rest arrive in order), with
+    lengths 1 + Zipf(1.2) capped at 256 over a hidden model; each clause has
+    a latent report rate r ~ Beta(0.5, 20) and LBD = round(length * U) with
+    U in [0.3, 1] falling with r (U = 0.3 + 0.7 * clip(1 - 10 r + 0.15 N(0,1))).
+    The base state: n_words words of 32 slots, each slot assigning each
+    variable with probability `assigned`, always to its model value, so no
+    clause reports unless planted (gss_bench_plant plants clause c at rate
+    r_c). Returns a dict of numpy arrays."""
+    rng = np.random.default_rng(seed)
+    total = n_clauses + stream
+    model = rng.integers(0, 2, size=n_vars).astype(np.uint8)
+    lengths = lengths_batching(rng, total)
+    lits, offsets = model_clauses(rng, lengths, n_vars, model)
+    r = rng.beta(0.5, 20, size=total).astype(np.float32)
+    u = np.clip(1 - 10 * r + 0.15 * rng.standard_normal(total), 0, 1)
+    lens = np.diff(offsets)
+    lbd = np.maximum(1, np.round(lens * (0.3 + 0.7 * u))).astype(np.uint16)
+    state = np.empty((n_vars, n_words, 2), dtype=np.uint32)
+    thr = np.uint32(int(assigned * 65536))
+    for w in range(n_words):
+        bits = (rng.integers(0, 65536, size=(n_vars, 32), dtype=np.uint32) < thr).astype(np.uint8)
+        state[:, w, 0] = np.packbits(bits, axis=1, bitorder="little").view("<u4").reshape(n_vars)
+    state[:, :, 1] = np.where(model[:, None] == 1, np.uint32(0xFFFFFFFF), np.uint32(0))
+    return {"lits": lits, "offsets": offsets, "rate": r, "lbd": lbd, "state": state, "model": model,
+            "n_vars": n_vars, "n_words": n_words, "n_clauses": n_clauses, "stream": stream}

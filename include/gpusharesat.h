@@ -138,6 +138,9 @@ int64_t gss_db_live_count(const gss_engine *eng);
 int64_t gss_db_literal_count(const gss_engine *eng);
 /* Largest variable index used by the database, -1 if empty. */
 int64_t gss_db_max_var(const gss_engine *eng);
+/* Position of each clause id in the plain scan order (-1: not in the
+ * database); positions change at gss_db_set and gss_db_compact. */
+int gss_db_positions(const gss_engine *eng, const uint32_t *ids, int64_t n, int64_t *positions);
 int gss_max_clause_len(void);
 
 /* ---- assignment state (replaces HostAssigs::fillAssigsAsync + dUpdateAssigs,
@@ -214,6 +217,94 @@ int gss_check_passes_host(gss_engine *eng, int n_passes, const uint32_t *const *
 int gss_check_noalloc(const int32_t *lits, const int64_t *offsets, uint32_t n_clauses, const uint32_t *state,
                       uint32_t n_vars, uint32_t n_blocks, const uint32_t *start, const int32_t *solver_of_word,
                       gss_report *out, uint32_t n_parts, uint32_t cap_per_part, uint32_t *counts_out, void *stream);
+
+/* ---- learned scan order (no counterpart in the reference) ----
+ * A 12-64-64-1 MLP scores every clause before each pass from 12 features:
+ * length, LBD, age, and the clause's report history (slot reports in each of
+ * the last 8 passes, total reports, passes since the last report). The pass
+ * then scans clauses in decreasing score, grouped by length within a score
+ * bucket, as two launches: the head (the first head_fraction of the scan),
+ * whose reports gss_check_wait_head returns while the tail still runs, and
+ * the tail. Every clause is still checked: the report set of a pass is the
+ * plain scan's. Weights are FP32; inference runs the two matrix layers on
+ * tensor cores with BF16 operands and FP32 accumulation. Training uses a log
+ * of (features, reported) rows sampled from past passes: every
+ * retrain_interval passes, train_epochs epochs of Adam on minibatches.
+ * The learned order runs the direct and wide kernels through
+ * gss_check_launch (not the tiled or persistent kernels, nor
+ * gss_check_passes_host). */
+typedef struct gss_order_params {
+    double head_fraction;      /* share of the scan in the head launch (default 0.1) */
+    int retrain_interval;      /* passes between trainings (default 1000; 0 = never automatically) */
+    int train_epochs;          /* epochs over the log per training (default 2) */
+    int batch;                 /* minibatch rows (default 4096) */
+    float learning_rate;       /* Adam step size (default 1e-3) */
+    int64_t log_capacity;      /* logged rows kept, newest first (default 2^20) */
+    double log_rate;           /* share of clauses logged per pass (0 = about 2000 rows a pass) */
+    uint64_t seed;             /* weight initialisation and minibatch sampling */
+} gss_order_params;
+
+void gss_order_params_default(gss_order_params *p);
+/* Enables the learned order for the next passes (p NULL = defaults); the
+ * history starts empty. */
+int gss_order_enable(gss_engine *eng, const gss_order_params *p);
+int gss_order_disable(gss_engine *eng);
+/* 0 = the next passes scan in the plain order and leave the history alone
+ * (for comparisons), 1 = learned order again. */
+int gss_order_set_active(gss_engine *eng, int on);
+/* LBD of clauses by id (0 = unknown, read as the length). */
+int gss_db_set_lbd(gss_engine *eng, const uint32_t *ids, const uint16_t *lbd, int64_t n);
+/* Waits for the head launch of the pass in flight and copies its reports
+ * (they are also among the pass's reports from gss_check_copy_reports). */
+int gss_check_wait_head(gss_engine *eng, gss_report *out, int64_t cap, int64_t *n_reports);
+typedef struct gss_order_stats {
+    int64_t passes;            /* ordered passes so far */
+    int64_t trainings;
+    double last_loss;          /* mean logistic loss of the last minibatch of the last training */
+    int64_t head_positions;    /* scan positions in the head of the last pass */
+    int64_t logged;            /* rows in the training log */
+    double score_ms;           /* device time of the last pass's history roll, scoring and sort */
+    double head_ms, tail_ms;   /* device time of its head and tail launches */
+} gss_order_stats;
+int gss_order_get_stats(gss_engine *eng, gss_order_stats *out);
+/* Trains now on the log, as the automatic retraining does. */
+int gss_order_train(gss_engine *eng);
+/* Features the next pass will score the given clauses with, x[n][12]. */
+int gss_order_clause_features(gss_engine *eng, const uint32_t *ids, int64_t n, float *x);
+/* The order's MLP weights (GSS_SCORER_PARAMS floats, layout as below). */
+int gss_order_get_weights(gss_engine *eng, float *w);
+int gss_order_set_weights(gss_engine *eng, const float *w);
+
+/* The MLP on its own. Flat FP32 weights: W1[64][12], b1[64], W2[64][64],
+ * b2[64], w3[64], b3 (5057 floats). */
+#define GSS_SCORER_FEATURES 12
+#define GSS_SCORER_HIDDEN 64
+#define GSS_SCORER_PARAMS 5057
+typedef struct gss_scorer gss_scorer;
+int gss_scorer_create(int device, uint64_t seed, gss_scorer **out);
+int gss_scorer_destroy(gss_scorer *s);
+int gss_scorer_get_weights(gss_scorer *s, float *w);
+int gss_scorer_set_weights(gss_scorer *s, const float *w);
+/* Logits of n rows of features x[n][12] (host memory): BF16 inference. */
+int gss_scorer_infer(gss_scorer *s, const float *x, int64_t n, float *logits);
+/* Mean logistic loss of rows x with labels y[n] in {0,1}, and its FP32
+ * gradient (GSS_SCORER_PARAMS floats); the weights do not change. */
+int gss_scorer_gradient(gss_scorer *s, const float *x, const float *y, int64_t n, float *grad, float *loss);
+/* One Adam step on rows x, labels y; *loss = the loss before the step. */
+int gss_scorer_train_step(gss_scorer *s, const float *x, const float *y, int64_t n, float lr, float *loss);
+
+/* ---- workload helper for the learned-order measurement ----
+ * Plants reports into an assignment state kept in device memory in the
+ * host-facing layout (uint32 state[n_vars][n_words][2]). Clause c of the
+ * device CSR (lits, offsets) is planted in this pass when a hash of
+ * (seed, pass, c) falls below rate[c]: in one slot picked by another hash,
+ * every literal but the last is made false and the last unassigned.
+ * restore = 1 puts back, from `base`, every state word the same call with
+ * restore = 0 touched. All pointers are device pointers; `stream` is a
+ * cudaStream_t (NULL = the default stream). */
+int gss_bench_plant(const int32_t *lits, const int64_t *offsets, int64_t n_clauses, const float *rate,
+                    uint32_t *state, const uint32_t *base, int64_t n_vars, int n_words, uint64_t seed, int64_t pass,
+                    int restore, void *stream);
 
 /* ---- the clause sharer: C form of GpuShare::GpuClauseSharer
  *      (gpuShareLib/GpuClauseSharer.h:74-163) ---- */

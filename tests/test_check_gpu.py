@@ -112,6 +112,15 @@ def test_empty_inputs(engine):
     assert len(_gpu_reports(engine, wl0)) == 0
 
 
+def test_wait_before_any_launch(lib):
+    """A fresh engine has no pass to wait for: wait and copy give nothing."""
+    import gpusharesat_gb300 as g
+    eng = g.Engine(0)
+    assert eng.wait() == 0
+    assert len(eng.reports()) == 0
+    eng.close()
+
+
 def test_overflow_reruns_to_same_result(engine):
     wl = W.make_small(seed=5, n_clauses=20000)
     ref = oracle.check(wl.lits, wl.offsets, wl.state, wl.start)
