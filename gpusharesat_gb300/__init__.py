@@ -97,6 +97,7 @@ def load():
     _sig(lib, "gss_order_set_active", c_int, vp, c_int)
     _sig(lib, "gss_db_set_lbd", c_int, vp, vp, vp, c_i64)
     _sig(lib, "gss_check_wait_head", c_int, vp, vp, c_i64, vp)
+    _sig(lib, "gss_check_copy_tail", c_int, vp, vp, c_i64, vp)
     _sig(lib, "gss_order_get_stats", c_int, vp, vp)
     _sig(lib, "gss_order_train", c_int, vp)
     _sig(lib, "gss_order_clause_features", c_int, vp, vp, c_i64, vp)
@@ -232,12 +233,14 @@ class Engine:
         _check(rc)
         return int(n.value)
 
-    def reports(self):
-        """Reports of the pass just waited for (no relaunch)."""
+    def reports(self, out=None):
+        """Reports of the pass just waited for (no relaunch), into `out` when
+        given and large enough."""
         n = self.wait()
         if n < 0:
             raise GssError(GSS_ERR_OVERFLOW, "report queues overflowed")
-        out = np.zeros(max(n, 1), dtype=REPORT_DTYPE)
+        if out is None or out.shape[0] < max(n, 1):
+            out = np.zeros(max(n, 1), dtype=REPORT_DTYPE)
         got = ctypes.c_int64()
         _check(self.lib.gss_check_copy_reports(self.h, _ptr(out), out.shape[0], ctypes.byref(got)))
         return out[:got.value]
@@ -284,12 +287,28 @@ class Engine:
         lbd = np.ascontiguousarray(lbd, dtype=np.uint16)
         _check(self.lib.gss_db_set_lbd(self.h, _ptr(ids), _ptr(lbd), ids.shape[0]))
 
-    def wait_head(self, cap=1 << 20):
-        """Reports of the head of the ordered pass in flight."""
+    def wait_head(self, cap=1 << 20, out=None):
+        """Reports of the head of the ordered pass in flight (into `out` when
+        given and large enough)."""
         while True:
-            out = np.zeros(max(int(cap), 1), dtype=REPORT_DTYPE)
+            if out is None or out.shape[0] < cap:
+                out = np.zeros(max(int(cap), 1), dtype=REPORT_DTYPE)
             n = ctypes.c_int64()
             rc = self.lib.gss_check_wait_head(self.h, _ptr(out), out.shape[0], ctypes.byref(n))
+            if rc == GSS_ERR_OVERFLOW and n.value > out.shape[0]:
+                cap = int(n.value)
+                continue
+            _check(rc)
+            return out[:n.value]
+
+    def copy_tail(self, cap=1 << 20, out=None):
+        """After wait_head: the rest of the pass's reports (into `out` when
+        given and large enough)."""
+        while True:
+            if out is None or out.shape[0] < cap:
+                out = np.zeros(max(int(cap), 1), dtype=REPORT_DTYPE)
+            n = ctypes.c_int64()
+            rc = self.lib.gss_check_copy_tail(self.h, _ptr(out), out.shape[0], ctypes.byref(n))
             if rc == GSS_ERR_OVERFLOW and n.value > out.shape[0]:
                 cap = int(n.value)
                 continue
@@ -347,7 +366,7 @@ class OrderParams(ctypes.Structure):
     """gss_order_params."""
     _fields_ = [("head_fraction", ctypes.c_double), ("retrain_interval", ctypes.c_int), ("train_epochs", ctypes.c_int),
                 ("batch", ctypes.c_int), ("learning_rate", ctypes.c_float), ("log_capacity", ctypes.c_int64),
-                ("log_rate", ctypes.c_double), ("seed", ctypes.c_uint64)]
+                ("log_rate", ctypes.c_double), ("seed", ctypes.c_uint64), ("overlap", ctypes.c_int)]
 
 
 class OrderStats(ctypes.Structure):

@@ -224,11 +224,14 @@ def learned(args):
     start = torch.full((n_words,), -1, dtype=torch.int32, device=dev)
     eng = g.Engine(0)
     eng.set_db(lits[:offsets[n0]], offsets[:n0 + 1])
-    eng.order_enable(head_fraction=args.head_fraction, retrain_interval=args.retrain, train_epochs=2, seed=4)
+    eng.order_enable(head_fraction=args.head_fraction, retrain_interval=args.retrain, train_epochs=2, seed=4,
+                     overlap=args.overlap)
     eng.set_lbd(np.arange(n0, dtype=np.uint32), d["lbd"][:n0])
     eng.set_capacity(1 << 22)
     lo, nxt = 0, n0
     rows = []
+    # report buffers reused across passes (their pages stay mapped)
+    bufs = [np.ones(1 << 22, dtype=g.REPORT_DTYPE) for _ in range(3)]
     for p in range(P):
         if p > 0 and k:
             ids = np.arange(nxt, nxt + k, dtype=np.uint32)
@@ -247,10 +250,11 @@ def learned(args):
         eng.wait()
         ta = time.perf_counter()
         eng.launch()
-        head = eng.wait_head()
+        head = eng.wait_head(cap=bufs[0].shape[0], out=bufs[0])
         tb = time.perf_counter()
-        full = eng.reports()
+        tail = eng.copy_tail(cap=bufs[1].shape[0], out=bufs[1])
         tc = time.perf_counter()
+        full = np.concatenate([head, tail])
         st = eng.order_stats()
         row = {"pass": p, "head_bits": _bits(head), "bits": _bits(full), "head_ms": (tb - ta) * 1e3,
                "all_ms": (tc - ta) * 1e3, "score_dev_ms": st["score_ms"], "head_dev_ms": st["head_ms"],
@@ -261,7 +265,7 @@ def learned(args):
             eng.kernel_time()
             td = time.perf_counter()
             eng.launch()
-            plain = eng.reports()
+            plain = eng.reports(out=bufs[2])
             te = time.perf_counter()
             row["plain_all_ms"] = (te - td) * 1e3
             row["plain_dev_ms"] = eng.kernel_time()[0]
@@ -307,6 +311,10 @@ def learned(args):
                "pass_ms_learned": float(np.mean([r["all_ms"] for r in cmp_rows])) if cmp_rows else None,
                "pass_ms_plain": float(np.mean([r["plain_all_ms"] for r in cmp_rows])) if cmp_rows else None,
                "score_dev_ms": float(np.mean([r["score_dev_ms"] for r in trained])) if trained else None,
+               "device_ms_learned": float(np.mean([r["score_dev_ms"] + r["head_dev_ms"] + r["tail_dev_ms"]
+                                                   for r in cmp_rows])) if cmp_rows else None,
+               "device_ms_plain": float(np.mean([r["plain_dev_ms"] for r in cmp_rows])) if cmp_rows else None,
+               "overlap": args.overlap,
                "checks_per_s_learned": float(np.mean(checks_ordered)) if cmp_rows else None,
                "checks_per_s_plain": float(np.mean(checks_plain)) if cmp_rows else None,
                "same_reports_every_compared_pass": all(r["same_reports"] for r in rows if "same_reports" in r),
@@ -329,6 +337,7 @@ def main(argv=None):
     p.add_argument("--retrain", type=int, default=1000)
     p.add_argument("--head-fraction", type=float, default=0.1)
     p.add_argument("--compare-every", type=int, default=5)
+    p.add_argument("--overlap", type=int, default=1)
     args = p.parse_args(argv)
     if args.config == "learned" and "--clauses" not in (argv or sys.argv):
         args.clauses = 4_000_000

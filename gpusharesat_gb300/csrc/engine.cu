@@ -139,7 +139,13 @@ int gss_engine_create(int device, gss_engine **out) {
     int rc = ensure_device(eng);
     if (rc == GSS_OK) {
         cudaError_t e = cudaDeviceGetAttribute(&eng->sm_count, cudaDevAttrMultiProcessorCount, device);
-        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&eng->own_stream, cudaStreamNonBlocking);
+        // the engine's own stream at the highest priority: its check kernels
+        // go before work of lower priority, such as the learned order's
+        // scoring of the next pass
+        int least = 0, greatest = 0;
+        if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+        if (e == cudaSuccess)
+            e = cudaStreamCreateWithPriority(&eng->own_stream, cudaStreamNonBlocking, greatest);
         if (e != cudaSuccess) rc = set_error(GSS_ERR_CUDA, "engine setup failed: %s", cudaGetErrorString(e));
     }
     if (rc != GSS_OK) {
@@ -328,6 +334,7 @@ int gss_db_set(gss_engine *eng, const int32_t *lits, const int64_t *offsets, int
     if (n_clauses > 0xFFFFFFF0LL) return set_error(GSS_ERR_INVALID, "too many clauses (%lld)", (long long) n_clauses);
     int64_t max_var = -1;
     GSS_TRY(validate_batch(lits, offsets, n_clauses, max_var));
+    order_quiesce(eng);
     if (n_clauses > 0 && offsets[n_clauses] > 0x7FFFFF00LL)
         return set_error(GSS_ERR_INVALID, "too many literals (%lld)", (long long) offsets[n_clauses]);
     eng->h_lits.clear();
@@ -336,6 +343,7 @@ int gss_db_set(gss_engine *eng, const int32_t *lits, const int64_t *offsets, int
     eng->index_of.clear();
     eng->next_id = 0;
     eng->db_epoch++;
+    eng->layout_epoch++;
     mirror_append(eng, lits, offsets, n_clauses, nullptr);
     GSS_TRY(upload_all(eng));
     eng->max_var = max_var;
@@ -346,6 +354,7 @@ int gss_db_append(gss_engine *eng, const int32_t *lits, const int64_t *offsets, 
                   const uint32_t *ids) {
     if (!eng || !offsets || n_clauses < 0) return set_error(GSS_ERR_INVALID, "bad arguments to gss_db_append");
     if (n_clauses == 0) return GSS_OK;
+    order_quiesce(eng);
     int64_t max_var = -1;
     GSS_TRY(validate_batch(lits, offsets, n_clauses, max_var));
     const int64_t first = (int64_t) eng->h_ids.size();
@@ -387,6 +396,7 @@ int gss_db_append(gss_engine *eng, const int32_t *lits, const int64_t *offsets, 
 
 int gss_db_delete(gss_engine *eng, const uint32_t *ids, int64_t n) {
     if (!eng || n < 0 || (n > 0 && !ids)) return set_error(GSS_ERR_INVALID, "bad arguments to gss_db_delete");
+    order_quiesce(eng);
     int64_t missing = 0;
     for (int64_t k = 0; k < n; k++) {
         const uint32_t id = ids[k];
@@ -409,6 +419,8 @@ int gss_db_delete(gss_engine *eng, const uint32_t *ids, int64_t n) {
 int gss_db_compact(gss_engine *eng) {
     if (!eng) return set_error(GSS_ERR_INVALID, "engine is NULL");
     if (eng->n_dead == 0) return GSS_OK;
+    order_quiesce(eng);
+    eng->layout_epoch++;
     // the live clauses, re-sorted by length (stable)
     std::vector<int32_t> lits;
     std::vector<int64_t> off(1, 0);
@@ -613,6 +625,7 @@ int gss_check_launch(gss_engine *eng) {
 namespace {
 
 int launch_pass_into(gss_engine *eng, const void *state, DevBuf &reports, DevBuf &counts, PinnedBuf &h_counts) {
+    order_quiesce(eng);  // a scoring in flight reads the buffers this pass may reallocate
     if (eng->n_clauses > 0 && eng->max_var >= eng->n_vars)
         return set_error(GSS_ERR_INVALID, "database uses variable %lld but the state has %lld variables",
                          (long long) eng->max_var, (long long) eng->n_vars);
@@ -746,15 +759,21 @@ int launch_pass_into(gss_engine *eng, const void *state, DevBuf &reports, DevBuf
     if (ordered) {
         // learned order: score and sort, then the head of the scan, its
         // counts for early delivery, the tail, and the history update
-        uint32_t head = 0;
-        GSS_TRY(order_prepare(eng, &a.perm, &head));
+        uint32_t head = 0, covered = 0;
+        GSS_TRY(order_prepare(eng, &a.perm, &head, &covered));
         a.scan_begin = 0;
         a.scan_end = head;
         if (head) GSS_TRY(launch(a));
         GSS_TRY(order_after_head(eng, counts));
         a.scan_begin = head;
-        a.scan_end = a.n_clauses;
-        if (head < a.n_clauses) GSS_TRY(launch(a));
+        a.scan_end = covered;
+        if (head < covered) GSS_TRY(launch(a));
+        if (covered < a.n_clauses) {  // appended since the order was computed
+            a.perm = nullptr;
+            a.scan_begin = covered;
+            a.scan_end = a.n_clauses;
+            GSS_TRY(launch(a));
+        }
         GSS_TRY(order_after_pass(eng, reports, counts));
     } else {
         GSS_TRY(launch(a));

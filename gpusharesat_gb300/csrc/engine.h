@@ -90,17 +90,23 @@ struct gss_engine {
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_pending;
 
     // learned scan order (NULL: plain length-sorted scan); db_epoch counts
-    // gss_db_set calls, so the order knows when clause ids start over
+    // gss_db_set calls, so the order knows when clause ids start over;
     gss::OrderState *order = nullptr;
     uint64_t db_epoch = 0;
+    uint64_t layout_epoch = 0;  // counts gss_db_set and gss_db_compact (positions change)
 };
 
 
 namespace gss {
 // Learned scan order hooks, called by the engine's pass (order.cu).
-// Before the scan: scores every clause and builds the scan permutation;
-// *head = scan positions in the head. Enqueued on the engine's stream.
-int order_prepare(gss_engine *eng, const uint32_t **perm, uint32_t *head);
+// Before the scan: the scan permutation of this pass (computed while the
+// previous pass ran, or now on the engine's stream). It covers positions
+// [0, *covered); *head = scan positions in the head. Clauses appended after
+// it was computed (positions from *covered on) are scanned after it.
+int order_prepare(gss_engine *eng, const uint32_t **perm, uint32_t *head, uint32_t *covered);
+// Waits until no scoring for a coming pass reads the engine's buffers; every
+// call that frees, moves or rewrites them calls this first.
+void order_quiesce(gss_engine *eng);
 // After the head launch: records the head's report counts for early delivery.
 int order_after_head(gss_engine *eng, const DevBuf &counts);
 // After the tail launch: folds the pass's reports into the report history.

@@ -3,7 +3,7 @@
 // are checked, and their reports delivered, first. Every clause is still
 // checked each pass: the report set is the plain scan's.
 //
-// Per pass (order_prepare, all on the engine's stream):
+// Per pass (score_pass):
 //   1-2. score_kernel, one warp per 16 clause positions: folds each clause's
 //      report count of the previous pass into its 8-pass history (a byte per
 //      pass; the first time an id is seen, its birth), logs a sample of
@@ -17,7 +17,12 @@
 //      order (lane groups of a warp keep clauses of one length, as in the
 //      plain scan)
 // After the pass (order_after_pass): history_kernel adds each report's slot
-// count to its clause's counter for the pass.
+// count to its clause's counter for the pass, and the scoring of the next
+// pass is enqueued on a stream of its own, behind the head of this pass: it
+// runs while the tail of this pass runs, so a pass usually starts with its
+// order ready. The scoring of pass q therefore sees reports up to pass q-2
+// (each clause keeps two counters, for even and odd passes). Calls that
+// change the engine's buffers wait for it first (order_quiesce).
 //
 // Training (every retrain_interval passes, and gss_scorer_train_step): FP32
 // forward and backward kernels over a minibatch, a gradient kernel (one
@@ -107,19 +112,24 @@ struct alignas(32) ClauseRecord {  // field order is read as two uint4 by score_
     uint64_t hist;   // byte k = slot reports in pass (now - 1 - k), saturated at 255
     uint32_t total;  // slot reports over the clause's life
     int32_t last;    // pass of the last report, -1 never
-    int32_t birth;   // pass the clause was first scored in
-    uint32_t cur;    // slot reports in the pass being run (added by history_kernel)
+    int32_t birth;   // the `now` of the first scoring that saw the clause
+    uint32_t cur0;   // slot reports of the last even pass not yet folded in (history_kernel)
     uint16_t lbd;    // 0 = unknown (read as the length)
-    uint16_t pad0;
-    uint32_t pad1;
+    uint16_t pad;
+    uint32_t cur1;   // the same for odd passes
 };
 static_assert(sizeof(ClauseRecord) == 32, "one sector per clause");
 
+// Scoring for pass q folds the counts of pass q-2 (slot q & 1) into the
+// history: pass q-1 may still be running when pass q is scored. Features
+// are then those of a prediction for the pass after `now` = q-1.
 struct HistoryArgs {
     ClauseRecord *rec;
     uint32_t n_ids;
-    uint32_t known_ids;  // ids below this existed at the previous pass
-    int32_t now;         // this pass
+    uint32_t known_ids;  // ids below this were seen by an earlier scoring
+    int32_t now;         // q - 1
+    int32_t fold;        // the pass whose counts are folded, q - 2 (negative: none)
+    uint32_t slot;       // its count slot, q & 1
 };
 
 // ------------------------------------------------------------ the scorer
@@ -168,13 +178,16 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], uint32_t a0, uint32_t a1
 }
 
 struct MlpShared {
+    uint2 w1[8][32];   // layer-1 fragments [tile][lane]
     uint2 w2[32][32];  // layer-2 fragments [tile][lane]
     float b1[kH], b2[kH], w3[kH];
     float b3;
 };
 
 __device__ void load_mlp_shared(MlpShared &sm, const float *w, const uint32_t *frag) {
-    const uint2 *f2 = reinterpret_cast<const uint2 *>(frag) + kFrag1;
+    const uint2 *f1 = reinterpret_cast<const uint2 *>(frag);
+    for (int i = threadIdx.x; i < kFrag1; i += blockDim.x) sm.w1[i >> 5][i & 31] = f1[i];
+    const uint2 *f2 = f1 + kFrag1;
     for (int i = threadIdx.x; i < kFrag2; i += blockDim.x) sm.w2[i >> 5][i & 31] = f2[i];
     for (int i = threadIdx.x; i < kH; i += blockDim.x) {
         sm.b1[i] = w[oB1 + i];
@@ -186,39 +199,26 @@ __device__ void load_mlp_shared(MlpShared &sm, const float *w, const uint32_t *f
 
 // One warp, 16 rows: lane (g = lane/4, t = lane%4) brings the features of
 // rows g and g+8 and gets back both logits (every lane of the group).
-__device__ __forceinline__ void mlp16(const float (&x0)[kF], const float (&x1)[kF], const uint2 (&w1f)[8],
-                                      const MlpShared &sm, float &out0, float &out1) {
+// v: columns 2t, 2t+1, 2t+8, 2t+9 of rows g (v[0..3]) and g+8 (v[4..7]).
+__device__ __forceinline__ void mlp16v(const float (&v)[8], const MlpShared &sm, float &out0, float &out1) {
     const int lane = threadIdx.x & 31, t = lane & 3;
-    float v[8];  // columns 2t, 2t+1, 2t+8, 2t+9 of rows g and g+8
-#pragma unroll
-    for (int q = 0; q < 8; q++) v[q] = 0.0f;
-#pragma unroll
-    for (int c = 0; c < kF; c++) {
-        if (c == 2 * t) v[0] = x0[c], v[4] = x1[c];
-        if (c == 2 * t + 1) v[1] = x0[c], v[5] = x1[c];
-        if (c == 2 * t + 8) v[2] = x0[c], v[6] = x1[c];
-        if (c == 2 * t + 9) v[3] = x0[c], v[7] = x1[c];
-    }
     const uint32_t a0 = pack_bf16(v[0], v[1]), a1 = pack_bf16(v[4], v[5]);
     const uint32_t a2 = pack_bf16(v[2], v[3]), a3 = pack_bf16(v[6], v[7]);
-    float d1[8][4];
-#pragma unroll
-    for (int nt = 0; nt < 8; nt++) {
-        d1[nt][0] = d1[nt][1] = d1[nt][2] = d1[nt][3] = 0.0f;
-        mma_bf16(d1[nt], a0, a1, a2, a3, w1f[nt].x, w1f[nt].y);
-    }
-    // bias + ReLU, re-packed as the A operand of layer 2 (the accumulator
-    // layout of n-tiles 2kt and 2kt+1 is the A layout of k-tile kt)
+    // layer 1 one k-tile of layer 2 at a time (n-tiles 2kt and 2kt+1): bias
+    // + ReLU, re-packed as the A operand of layer 2 (the accumulator layout
+    // of n-tiles 2kt and 2kt+1 is the A layout of k-tile kt)
     uint32_t h[4][4];
 #pragma unroll
     for (int kt = 0; kt < 4; kt++) {
+        float p0[4] = {0.0f, 0.0f, 0.0f, 0.0f}, p1[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        const uint2 b0 = sm.w1[2 * kt][lane], b1 = sm.w1[2 * kt + 1][lane];
+        mma_bf16(p0, a0, a1, a2, a3, b0.x, b0.y);
+        mma_bf16(p1, a0, a1, a2, a3, b1.x, b1.y);
         const int c0 = 16 * kt + 2 * t, c1 = c0 + 8;
-        h[kt][0] = pack_bf16(fmaxf(d1[2 * kt][0] + sm.b1[c0], 0.0f), fmaxf(d1[2 * kt][1] + sm.b1[c0 + 1], 0.0f));
-        h[kt][1] = pack_bf16(fmaxf(d1[2 * kt][2] + sm.b1[c0], 0.0f), fmaxf(d1[2 * kt][3] + sm.b1[c0 + 1], 0.0f));
-        h[kt][2] = pack_bf16(fmaxf(d1[2 * kt + 1][0] + sm.b1[c1], 0.0f),
-                             fmaxf(d1[2 * kt + 1][1] + sm.b1[c1 + 1], 0.0f));
-        h[kt][3] = pack_bf16(fmaxf(d1[2 * kt + 1][2] + sm.b1[c1], 0.0f),
-                             fmaxf(d1[2 * kt + 1][3] + sm.b1[c1 + 1], 0.0f));
+        h[kt][0] = pack_bf16(fmaxf(p0[0] + sm.b1[c0], 0.0f), fmaxf(p0[1] + sm.b1[c0 + 1], 0.0f));
+        h[kt][1] = pack_bf16(fmaxf(p0[2] + sm.b1[c0], 0.0f), fmaxf(p0[3] + sm.b1[c0 + 1], 0.0f));
+        h[kt][2] = pack_bf16(fmaxf(p1[0] + sm.b1[c1], 0.0f), fmaxf(p1[1] + sm.b1[c1 + 1], 0.0f));
+        h[kt][3] = pack_bf16(fmaxf(p1[2] + sm.b1[c1], 0.0f), fmaxf(p1[3] + sm.b1[c1 + 1], 0.0f));
     }
     float s0 = 0.0f, s1 = 0.0f;
 #pragma unroll
@@ -241,12 +241,22 @@ __device__ __forceinline__ void mlp16(const float (&x0)[kF], const float (&x1)[k
     out1 = s1 + sm.b3;
 }
 
-__device__ __forceinline__ void load_w1_frags(const uint32_t *frag, uint2 (&w1f)[8]) {
-    const uint2 *f1 = reinterpret_cast<const uint2 *>(frag);
-    const int lane = threadIdx.x & 31;
+__device__ __forceinline__ void mlp16(const float (&x0)[kF], const float (&x1)[kF], const MlpShared &sm,
+                                      float &out0, float &out1) {
+    const int t = threadIdx.x & 3;
+    float v[8];
 #pragma unroll
-    for (int nt = 0; nt < 8; nt++) w1f[nt] = f1[nt * 32 + lane];
+    for (int q = 0; q < 8; q++) v[q] = 0.0f;
+#pragma unroll
+    for (int c = 0; c < kF; c++) {
+        if (c == 2 * t) v[0] = x0[c], v[4] = x1[c];
+        if (c == 2 * t + 1) v[1] = x0[c], v[5] = x1[c];
+        if (c == 2 * t + 8) v[2] = x0[c], v[6] = x1[c];
+        if (c == 2 * t + 9) v[3] = x0[c], v[7] = x1[c];
+    }
+    mlp16v(v, sm, out0, out1);
 }
+
 
 constexpr int kMlpThreads = 256;
 
@@ -258,8 +268,6 @@ __global__ void __launch_bounds__(kMlpThreads) infer_rows_kernel(const float *__
     __shared__ MlpShared sm;
     load_mlp_shared(sm, w, frag);
     __syncthreads();
-    uint2 w1f[8];
-    load_w1_frags(frag, w1f);
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
     const uint32_t warps = gridDim.x * (blockDim.x >> 5);
     for (uint32_t tile = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); tile * 16 < n; tile += warps) {
@@ -271,7 +279,7 @@ __global__ void __launch_bounds__(kMlpThreads) infer_rows_kernel(const float *__
             x1[c] = r1 < n ? x[(size_t) r1 * kF + c] : 0.0f;
         }
         float o0, o1;
-        mlp16(x0, x1, w1f, sm, o0, o1);
+        mlp16(x0, x1, sm, o0, o1);
         if (t == 0) {
             if (r0 < n) out[r0] = o0;
             if (r1 < n) out[r1] = o1;
@@ -497,10 +505,22 @@ struct OrderState {
     int64_t cap_ids = 0;
     DevBuf rec;                                 // ClauseRecord per clause id
     DevBuf lbd_pairs;                           // staging of gss_db_set_lbd
-    DevBuf bucket, perm, offs, totals;          // per position; per (bucket, sort tile); per bucket
+    DevBuf bucket, offs, totals;                // per position; per (bucket, sort tile); per bucket
+    DevBuf perm[2];                             // scan permutation of passes with even / odd numbers
+    // the order of the next pass, computed on score_stream while the tail of
+    // the current pass runs (pre_*: what it was computed for)
+    cudaStream_t score_stream = nullptr;
+    cudaEvent_t ev_score_done = nullptr;
+    bool pre_ready = false, pre_in_flight = false;
+    int64_t pre_pass = -1;
+    int64_t folded_pass = -1;  // the last pass q whose scoring folded pass q-2's counts
+    uint32_t pre_n = 0;
+    uint64_t pre_layout = 0;
     DevBuf log_x, log_y, log_count;
     PinnedBuf h_head_counts, h_log_count;
-    cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};  // score start/end, head end, tail end, head counts
+    // score start/end, head end, tail end, head counts copied, head start
+    cudaEvent_t ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    uint32_t scored_n = 0;  // positions covered by the permutation of the pass in flight
     bool have_times = false;
     uint32_t head = 0;
     bool pending = false;  // a pass with a head launch is in flight
@@ -527,42 +547,38 @@ struct LogArgs {
     uint64_t seed;
 };
 
-// One warp per 16 positions. For each live clause: folds the previous pass's
-// report count into its history (the first time an id is seen: its birth),
-// logs a sample of (features before the fold, reported) rows, then scores
-// the clause with the features after the fold and writes its bucket.
-__global__ void __launch_bounds__(kMlpThreads) score_kernel(HistoryArgs h, LogArgs lg, const float *__restrict__ w,
-                                                            const uint32_t *__restrict__ frag,
-                                                            const int64_t *__restrict__ offsets,
-                                                            const uint32_t *__restrict__ orig,
-                                                            const uint32_t *__restrict__ alive, uint32_t n,
-                                                            uint8_t *__restrict__ bucket) {
+// One warp per 32 positions, a lane per position. For each live clause:
+// folds the report count of pass h.fold into its history (the first time an
+// id is seen: its birth), logs a sample of (features before the fold,
+// reported) rows, computes its features; then the lanes pass the features to
+// the MLP's fragment layout (two m16 tiles) and each lane writes its
+// clause's score bucket.
+__global__ void __launch_bounds__(kMlpThreads, 3) score_kernel(HistoryArgs h, LogArgs lg, const float *__restrict__ w,
+                                                               const uint32_t *__restrict__ frag,
+                                                               const int64_t *__restrict__ offsets,
+                                                               const uint32_t *__restrict__ orig,
+                                                               const uint32_t *__restrict__ alive, uint32_t n,
+                                                               uint8_t *__restrict__ bucket) {
     __shared__ MlpShared sm;
+    __shared__ float xs[kMlpThreads / 32][32][kF + 1];  // each warp's rows of features
     load_mlp_shared(sm, w, frag);
     __syncthreads();
-    uint2 w1f[8];
-    load_w1_frags(frag, w1f);
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    float(*wx)[kF + 1] = xs[threadIdx.x >> 5];
     const uint32_t warps = gridDim.x * (blockDim.x >> 5);
-    const int32_t prev = h.now - 1;
-    for (uint32_t tile = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); tile * 16 < n; tile += warps) {
-        const uint32_t r[2] = {tile * 16 + g, tile * 16 + g + 8};
-        float x0[kF], x1[kF];
-        bool live[2] = {false, false};
-        auto fill = [&](int q, float(&x)[kF]) {
+    for (uint32_t tile = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); tile * 32 < n; tile += warps) {
+        const uint32_t r = tile * 32 + lane;
+        float x[kF];
 #pragma unroll
-            for (int k = 0; k < kF; k++) x[k] = 0.0f;
-            if (r[q] >= n) return;
-            live[q] = alive == nullptr || ((alive[r[q] >> 5] >> (r[q] & 31)) & 1u);
-            const uint32_t id = orig[r[q]];
-            if (!live[q] || id >= h.n_ids) {
-                live[q] = false;
-                return;
-            }
-            const uint32_t len = (uint32_t) (offsets[r[q] + 1] - offsets[r[q]]);
-            // the record as two 16-byte words: {hist lo, hist hi, total, last}, {birth, cur, lbd|pad0, pad1}
-            const uint4 *rp = reinterpret_cast<const uint4 *>(h.rec + id);
-            const uint4 ra = rp[0], rb = rp[1];
+        for (int k = 0; k < kF; k++) x[k] = 0.0f;
+        bool live = r < n && (alive == nullptr || ((alive[r >> 5] >> (r & 31)) & 1u));
+        const uint32_t id = r < n ? orig[r] : 0u;
+        live = live && id < h.n_ids;
+        if (live) {
+            const uint32_t len = (uint32_t) (offsets[r + 1] - offsets[r]);
+            // the record as two 16-byte words: {hist lo, hist hi, total, last}, {birth, cur0, lbd|pad, cur1}
+            ClauseRecord *rec = h.rec + id;
+            const uint4 ra = reinterpret_cast<const uint4 *>(rec)[0], rb = reinterpret_cast<const uint4 *>(rec)[1];
             const uint32_t lbd = rb.z & 0xFFFFu;
             int32_t birth, last;
             uint64_t hist;
@@ -572,38 +588,65 @@ __global__ void __launch_bounds__(kMlpThreads) score_kernel(HistoryArgs h, LogAr
                 birth = h.now, last = -1, hist = 0, total = 0;
             } else {
                 birth = (int32_t) rb.x, last = (int32_t) ra.w, hist = ((uint64_t) ra.y << 32) | ra.x, total = ra.z;
-                const uint32_t c = rb.y;
-                if (t == 0 && lg.cap && prev >= 0 && birth <= prev && unit_hash(lg.seed, (uint64_t) prev, id) < lg.rate) {
+                const uint32_t c = h.fold >= 0 ? (h.slot ? rb.w : rb.y) : 0u;
+                // a training row: the features a prediction for pass `fold`
+                // would have used, and whether the clause reported in it
+                if (lg.cap && h.fold >= 0 && birth < h.fold && unit_hash(lg.seed, (uint64_t) h.fold, id) < lg.rate) {
                     float xl[kF];
-                    clause_features(len, lbd, prev - birth, hist, total, last < 0 ? -1 : prev - last, xl);
+                    clause_features(len, lbd, h.fold - birth, hist, total, last < 0 ? -1 : h.fold - last, xl);
                     const unsigned long long slot = atomicAdd(lg.count, 1ull) % lg.cap;
 #pragma unroll
                     for (int k = 0; k < kF; k++) lg.x[slot * kF + k] = xl[k];
                     lg.y[slot] = c ? 1.0f : 0.0f;
                 }
-                hist = (hist << 8) | (uint64_t) (c < 255u ? c : 255u);
-                total += c;
-                if (c) last = prev;
+                if (h.fold >= 0) {
+                    hist = (hist << 8) | (uint64_t) (c < 255u ? c : 255u);
+                    total += c;
+                    if (c) last = h.fold;
+                }
             }
-            __syncwarp(0xFu << (lane & ~3));  // the group's reads before its writer's stores
-            if (t == 0) {
-                uint4 *wp = reinterpret_cast<uint4 *>(h.rec + id);
-                wp[0] = make_uint4((uint32_t) hist, (uint32_t) (hist >> 32), total, (uint32_t) last);
-                wp[1] = make_uint4((uint32_t) birth, 0u, rb.z, rb.w);  // cur = 0
+            // the history word and the folded slot; the other slot may be
+            // taking the counts of the pass in flight (history_kernel)
+            *reinterpret_cast<uint4 *>(rec) = make_uint4((uint32_t) hist, (uint32_t) (hist >> 32), total,
+                                                         (uint32_t) last);
+            if (born) rec->birth = birth;
+            if (h.fold >= 0) {
+                if (h.slot)
+                    rec->cur1 = 0;
+                else
+                    rec->cur0 = 0;
             }
             clause_features(len, lbd, h.now - birth, hist, total, last < 0 ? -1 : h.now - last, x);
-        };
-        fill(0, x0);
-        fill(1, x1);
-        float o[2];
-        mlp16(x0, x1, w1f, sm, o[0], o[1]);
-        if (t == 0) {
-#pragma unroll
-            for (int q = 0; q < 2; q++) {
-                if (r[q] >= n) continue;
-                bucket[r[q]] = (uint8_t) (live[q] ? bucket_of(o[q]) : (uint32_t) (kBuckets - 1));
-            }
         }
+        // two m16 tiles: rows 0-15 and 16-31 of the warp's positions, their
+        // features passed to the fragment layout through shared memory
+#pragma unroll
+        for (int k = 0; k < kF; k++) wx[lane][k] = x[k];
+        __syncwarp();
+        float logit = 0.0f;
+#pragma unroll 1
+        for (int sub = 0; sub < 2; sub++) {
+            const float *f0 = wx[sub * 16 + g], *f1 = wx[sub * 16 + g + 8];
+            const int c = 2 * t;
+            float v[8];
+            v[0] = f0[c];
+            v[1] = f0[c + 1];
+            v[2] = c + 8 < kF ? f0[c + 8] : 0.0f;
+            v[3] = c + 9 < kF ? f0[c + 9] : 0.0f;
+            v[4] = f1[c];
+            v[5] = f1[c + 1];
+            v[6] = c + 8 < kF ? f1[c + 8] : 0.0f;
+            v[7] = c + 9 < kF ? f1[c + 9] : 0.0f;
+            float o0, o1;
+            mlp16v(v, sm, o0, o1);
+            // back to the lane that owns the row: row i of the tile is in lanes 4(i%8)..
+            const int i = lane & 15;
+            const float a = __shfl_sync(kFullMask, o0, 4 * (i & 7));
+            const float b = __shfl_sync(kFullMask, o1, 4 * (i & 7));
+            if ((lane >> 4) == sub) logit = (i < 8) ? a : b;
+        }
+        if (r < n) bucket[r] = (uint8_t) (live ? bucket_of(logit) : (uint32_t) (kBuckets - 1));
+        __syncwarp();  // wx is rewritten by the next tile
     }
 }
 
@@ -707,13 +750,13 @@ __global__ void __launch_bounds__(kSortThreads) bucket_scatter_kernel(const uint
 
 __global__ void history_kernel(const gss_report *__restrict__ reports, const uint32_t *__restrict__ counts,
                                uint32_t n_parts, uint32_t cap_per_part, ClauseRecord *__restrict__ rec,
-                               uint32_t n_ids) {
+                               uint32_t n_ids, uint32_t slot) {
     for (uint32_t q = blockIdx.x; q < n_parts; q += gridDim.x) {
         const uint32_t m = min(counts[q], cap_per_part);
         const gss_report *r = reports + (size_t) q * cap_per_part;
         for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
             const uint32_t id = r[i].clause;
-            if (id < n_ids) atomicAdd(&rec[id].cur, (uint32_t) __popc(r[i].mask));
+            if (id < n_ids) atomicAdd(slot ? &rec[id].cur1 : &rec[id].cur0, (uint32_t) __popc(r[i].mask));
         }
     }
 }
@@ -827,6 +870,11 @@ void order_destroy(gss_engine *eng) {
         cudaStreamSynchronize(o->train_stream);
         cudaStreamDestroy(o->train_stream);
     }
+    if (o->score_stream) {
+        cudaStreamSynchronize(o->score_stream);
+        cudaStreamDestroy(o->score_stream);
+    }
+    if (o->ev_score_done) cudaEventDestroy(o->ev_score_done);
     for (cudaEvent_t &e : o->ev)
         if (e) cudaEventDestroy(e);
     if (o->ev_train_start) cudaEventDestroy(o->ev_train_start);
@@ -835,22 +883,28 @@ void order_destroy(gss_engine *eng) {
     eng->order = nullptr;
 }
 
-int order_prepare(gss_engine *eng, const uint32_t **perm, uint32_t *head) {
+void order_quiesce(gss_engine *eng) {
+    if (!eng->order || !eng->order->pre_in_flight) return;
+    cudaEventSynchronize(eng->order->ev_score_done);
+    eng->order->pre_in_flight = false;
+}
+
+namespace {
+
+// Enqueues on `st` the scoring and ordering of pass q over the database as it
+// is now, into perm[q & 1]; returns the positions covered.
+int score_pass(gss_engine *eng, cudaStream_t st, int64_t q, uint32_t *covered) {
     OrderState &o = *eng->order;
-    cudaStream_t st = eng->stream;
     const uint32_t n = (uint32_t) eng->n_clauses;
     const int64_t n_ids = eng->next_id;
-    if (o.epoch != eng->db_epoch) {  // a new database: forget the history
-        o.epoch = eng->db_epoch;
-        o.known_ids = 0;
-        if (o.cap_ids) GSS_CUDA_TRY(cudaMemsetAsync(o.rec.ptr, 0, (size_t) o.cap_ids * sizeof(ClauseRecord), st));
-    }
     GSS_TRY(ensure_ids(eng, std::max<int64_t>(n_ids, 1)));
-    GSS_TRY(train_finish(eng, false));
-    if (o.prm.retrain_interval > 0 && o.pass > 0 && o.pass % o.prm.retrain_interval == 0) GSS_TRY(train_start(eng));
     GSS_TRY(scorer_frags(&o.scorer, st));
     GSS_CUDA_TRY(cudaEventRecord(o.ev[0], st));
-    HistoryArgs h = history_args(eng, (int32_t) o.pass);
+    HistoryArgs h = history_args(eng, (int32_t) (q - 1));
+    // a pass's counts are folded once, by the first scoring of pass q
+    h.fold = o.folded_pass < q ? (int32_t) (q - 2) : -1;
+    h.slot = (uint32_t) (q & 1);
+    o.folded_pass = std::max(o.folded_pass, q);
     LogArgs lg;
     lg.x = (float *) o.log_x.ptr;
     lg.y = (float *) o.log_y.ptr;
@@ -859,19 +913,20 @@ int order_prepare(gss_engine *eng, const uint32_t **perm, uint32_t *head) {
     lg.rate = (float) std::min(1.0, o.prm.log_rate > 0 ? o.prm.log_rate
                                                         : 2000.0 / (double) std::max<int64_t>(n_ids, 1));
     lg.seed = o.prm.seed;
-    // 1-2. history fold, log, scores and buckets
+    DevBuf &perm = o.perm[q & 1];
     const uint32_t n_tiles = (uint32_t) (((size_t) n + kSortTile - 1) / kSortTile);
-    GSS_TRY(o.perm.reserve(std::max<size_t>(n, 1) * sizeof(uint32_t)));
+    GSS_TRY(perm.reserve(std::max<size_t>(n, 1) * sizeof(uint32_t)));
     GSS_TRY(o.bucket.reserve(std::max<size_t>(n, 1)));
     GSS_TRY(o.offs.reserve(std::max<size_t>((size_t) kBuckets * n_tiles, 1) * sizeof(uint32_t)));
     GSS_TRY(o.totals.reserve(kBuckets * sizeof(uint32_t)));
     if (n) {
-        score_kernel<<<grid_for_n((uint64_t) (n + 15) / 16 * 32, eng->sm_count, kMlpThreads), kMlpThreads, 0, st>>>(
+        // history fold, training log, features, MLP, score bucket
+        score_kernel<<<grid_for_n((uint64_t) (n + 31) / 32 * 32, eng->sm_count, kMlpThreads), kMlpThreads, 0, st>>>(
             h, lg, (const float *) o.scorer.w.ptr, (const uint32_t *) o.scorer.frag.ptr,
             (const int64_t *) eng->offsets.ptr, (const uint32_t *) eng->orig.ptr,
             eng->n_dead > 0 ? (const uint32_t *) eng->alive.ptr : nullptr, n, (uint8_t *) o.bucket.ptr);
         GSS_CUDA_TRY(cudaGetLastError());
-        // 3. stable radix sort of positions by bucket
+        // stable radix sort of positions by bucket
         bucket_hist_kernel<<<n_tiles, kSortThreads, 0, st>>>((const uint8_t *) o.bucket.ptr, n, n_tiles,
                                                               (uint32_t *) o.offs.ptr);
         GSS_CUDA_TRY(cudaGetLastError());
@@ -882,18 +937,50 @@ int order_prepare(gss_engine *eng, const uint32_t **perm, uint32_t *head) {
         bucket_scatter_kernel<<<n_tiles, kSortThreads, 0, st>>>((const uint8_t *) o.bucket.ptr, n, n_tiles,
                                                                  (const uint32_t *) o.offs.ptr,
                                                                  (const uint32_t *) o.totals.ptr,
-                                                                 (uint32_t *) o.perm.ptr);
+                                                                 (uint32_t *) perm.ptr);
         GSS_CUDA_TRY(cudaGetLastError());
     }
     GSS_CUDA_TRY(cudaEventRecord(o.ev[1], st));
     o.known_ids = n_ids;
-    o.pass++;
+    *covered = n;
+    return GSS_OK;
+}
+
+}  // namespace
+
+int order_prepare(gss_engine *eng, const uint32_t **perm, uint32_t *head, uint32_t *covered) {
+    OrderState &o = *eng->order;
+    cudaStream_t st = eng->stream;
+    order_quiesce(eng);
+    if (o.epoch != eng->db_epoch) {  // a new database: forget the history
+        o.epoch = eng->db_epoch;
+        o.known_ids = 0;
+        o.pre_ready = false;
+        o.folded_pass = o.pass - 1;  // nothing of the old database to fold
+        if (o.cap_ids) GSS_CUDA_TRY(cudaMemsetAsync(o.rec.ptr, 0, (size_t) o.cap_ids * sizeof(ClauseRecord), st));
+    }
+    GSS_TRY(ensure_ids(eng, std::max<int64_t>(eng->next_id, 1)));
+    const int64_t q = o.pass;
+    // new weights from a finished training; a training every retrain_interval passes
+    GSS_TRY(train_finish(eng, false));
+    if (o.prm.retrain_interval > 0 && q > 0 && q % o.prm.retrain_interval == 0) GSS_TRY(train_start(eng));
+    uint32_t n_scored = 0;
+    if (o.pre_ready && o.pre_pass == q && o.pre_layout == eng->layout_epoch) {
+        n_scored = o.pre_n;  // computed while the previous pass ran
+    } else {
+        GSS_TRY(score_pass(eng, st, q, &n_scored));
+    }
+    o.pre_ready = false;
+    o.pass = q + 1;
     double hf = o.prm.head_fraction;
     if (!(hf > 0.0)) hf = 0.0;
     if (hf > 1.0) hf = 1.0;
-    o.head = (uint32_t) std::min<double>((double) n, ceil(hf * (double) n));
-    *perm = (const uint32_t *) o.perm.ptr;
+    o.head = (uint32_t) std::min<double>((double) n_scored, ceil(hf * (double) n_scored));
+    o.scored_n = n_scored;
+    *perm = (const uint32_t *) o.perm[q & 1].ptr;
     *head = o.head;
+    *covered = n_scored;
+    GSS_CUDA_TRY(cudaEventRecord(o.ev[5], st));
     return GSS_OK;
 }
 
@@ -911,12 +998,25 @@ int order_after_head(gss_engine *eng, const DevBuf &counts) {
 int order_after_pass(gss_engine *eng, const DevBuf &reports, const DevBuf &counts) {
     OrderState &o = *eng->order;
     GSS_CUDA_TRY(cudaEventRecord(o.ev[3], eng->stream));
+    const int64_t q = o.pass - 1;  // the pass just enqueued
     history_kernel<<<eng->n_parts, 256, 0, eng->stream>>>((const gss_report *) reports.ptr,
                                                           (const uint32_t *) counts.ptr, eng->n_parts,
                                                           eng->cap_per_part, (ClauseRecord *) o.rec.ptr,
-                                                          (uint32_t) std::min<int64_t>(eng->next_id, o.cap_ids));
+                                                          (uint32_t) std::min<int64_t>(eng->next_id, o.cap_ids),
+                                                          (uint32_t) (q & 1));
     GSS_CUDA_TRY(cudaGetLastError());
     o.have_times = true;
+    // the order of pass q+1, on the scoring stream once the head of pass q is
+    // done (overlap) or pass q is: it folds the counts of pass q-1 (complete)
+    GSS_CUDA_TRY(cudaStreamWaitEvent(o.score_stream, o.prm.overlap ? o.ev[2] : o.ev[3], 0));
+    uint32_t covered = 0;
+    GSS_TRY(score_pass(eng, o.score_stream, q + 1, &covered));
+    GSS_CUDA_TRY(cudaEventRecord(o.ev_score_done, o.score_stream));
+    o.pre_in_flight = true;
+    o.pre_ready = true;
+    o.pre_pass = q + 1;
+    o.pre_n = covered;
+    o.pre_layout = eng->layout_epoch;
     return GSS_OK;
 }
 
@@ -941,6 +1041,7 @@ void gss_order_params_default(gss_order_params *p) {
     p->log_capacity = 1 << 20;
     p->log_rate = 0.0;
     p->seed = 1;
+    p->overlap = 1;
 }
 
 int gss_order_enable(gss_engine *eng, const gss_order_params *p) {
@@ -960,8 +1061,11 @@ int gss_order_enable(gss_engine *eng, const gss_order_params *p) {
     eng->order = o;
     int rc = scorer_init(&o->scorer, eng->device, prm.seed, eng->stream);
     if (rc == GSS_OK) rc = scorer_init(&o->trainer, eng->device, prm.seed, eng->stream);  // the same weights
-    for (int k = 0; rc == GSS_OK && k < 5; k++)
+    for (int k = 0; rc == GSS_OK && k < 6; k++)
         if (cudaEventCreate(&o->ev[k]) != cudaSuccess) rc = set_error(GSS_ERR_CUDA, "cudaEventCreate failed");
+    if (rc == GSS_OK && (cudaEventCreateWithFlags(&o->ev_score_done, cudaEventDisableTiming) != cudaSuccess ||
+                         cudaStreamCreateWithFlags(&o->score_stream, cudaStreamNonBlocking) != cudaSuccess))
+        rc = set_error(GSS_ERR_CUDA, "creating the scoring stream failed");
     if (rc == GSS_OK && (cudaEventCreateWithFlags(&o->ev_train_start, cudaEventDisableTiming) != cudaSuccess ||
                          cudaEventCreateWithFlags(&o->ev_train_done, cudaEventDisableTiming) != cudaSuccess ||
                          cudaStreamCreateWithFlags(&o->train_stream, cudaStreamNonBlocking) != cudaSuccess))
@@ -984,6 +1088,7 @@ int gss_order_enable(gss_engine *eng, const gss_order_params *p) {
 
 int gss_order_disable(gss_engine *eng) {
     if (!eng) return set_error(GSS_ERR_INVALID, "engine is NULL");
+    order_quiesce(eng);
     if (eng->pass_pending) return set_error(GSS_ERR_STATE, "a pass is in flight");
     order_destroy(eng);
     return GSS_OK;
@@ -991,6 +1096,7 @@ int gss_order_disable(gss_engine *eng) {
 
 int gss_order_set_active(gss_engine *eng, int on) {
     if (!eng) return set_error(GSS_ERR_INVALID, "engine is NULL");
+    order_quiesce(eng);
     if (!eng->order) return set_error(GSS_ERR_STATE, "the learned order is not enabled");
     if (eng->pass_pending) return set_error(GSS_ERR_STATE, "a pass is in flight");
     eng->order->active = on != 0;
@@ -1005,6 +1111,7 @@ int gss_db_set_lbd(gss_engine *eng, const uint32_t *ids, const uint16_t *lbd, in
     uint32_t max_id = 0;
     for (int64_t i = 0; i < n; i++) max_id = std::max(max_id, ids[i]);
     if (max_id >= eng->next_id) return set_error(GSS_ERR_NOT_FOUND, "clause id %u is not in the database", max_id);
+    order_quiesce(eng);
     GSS_TRY(ensure_ids(eng, eng->next_id));
     // (id, lbd) pairs up, then a scatter into the records
     OrderState &o = *eng->order;
@@ -1054,6 +1161,33 @@ int gss_check_wait_head(gss_engine *eng, gss_report *out, int64_t cap, int64_t *
     return GSS_OK;
 }
 
+int gss_check_copy_tail(gss_engine *eng, gss_report *out, int64_t cap, int64_t *n_reports) {
+    if (!eng || (cap > 0 && !out)) return set_error(GSS_ERR_INVALID, "bad arguments to gss_check_copy_tail");
+    if (!eng->order || !eng->order->active || !eng->order->pending)
+        return set_error(GSS_ERR_STATE, "no ordered pass whose head was taken");
+    int64_t total = 0;
+    GSS_TRY(gss_check_wait(eng, &total));
+    OrderState &o = *eng->order;
+    const uint32_t *hc = (const uint32_t *) o.h_head_counts.ptr;
+    const uint32_t *ac = (const uint32_t *) eng->h_counts.ptr;
+    int64_t n = 0;
+    for (uint32_t q = 0; q < eng->n_parts; q++) n += (int64_t) ac[q] - hc[q];
+    if (n_reports) *n_reports = n;
+    if (n > cap) return set_error(GSS_ERR_OVERFLOW, "output holds %lld records, the tail has %lld", (long long) cap,
+                                  (long long) n);
+    int64_t pos = 0;
+    for (uint32_t q = 0; q < eng->n_parts; q++) {
+        if (ac[q] == hc[q]) continue;
+        GSS_CUDA_TRY(cudaMemcpyAsync(out + pos,
+                                     (gss_report *) eng->reports.ptr + (size_t) q * eng->cap_per_part + hc[q],
+                                     (size_t) (ac[q] - hc[q]) * sizeof(gss_report), cudaMemcpyDeviceToHost,
+                                     eng->stream));
+        pos += ac[q] - hc[q];
+    }
+    GSS_CUDA_TRY(cudaStreamSynchronize(eng->stream));
+    return GSS_OK;
+}
+
 int gss_order_get_stats(gss_engine *eng, gss_order_stats *out) {
     if (!eng || !out) return set_error(GSS_ERR_INVALID, "bad arguments to gss_order_get_stats");
     if (!eng->order) return set_error(GSS_ERR_STATE, "the learned order is not enabled");
@@ -1069,9 +1203,10 @@ int gss_order_get_stats(gss_engine *eng, gss_order_stats *out) {
                                                           (unsigned long long) o.prm.log_capacity);
     if (o.have_times && !eng->pass_pending) {
         float a = 0, b = 0, c = 0;
+        order_quiesce(eng);
         GSS_CUDA_TRY(cudaEventSynchronize(o.ev[3]));
         GSS_CUDA_TRY(cudaEventElapsedTime(&a, o.ev[0], o.ev[1]));
-        GSS_CUDA_TRY(cudaEventElapsedTime(&b, o.ev[1], o.ev[2]));
+        GSS_CUDA_TRY(cudaEventElapsedTime(&b, o.ev[5], o.ev[2]));
         GSS_CUDA_TRY(cudaEventElapsedTime(&c, o.ev[2], o.ev[3]));
         out->score_ms = a;
         out->head_ms = b;
@@ -1085,6 +1220,7 @@ int gss_order_train(gss_engine *eng) {
     if (!eng->order) return set_error(GSS_ERR_STATE, "the learned order is not enabled");
     if (eng->pass_pending) return set_error(GSS_ERR_STATE, "a pass is in flight");
     GSS_CUDA_TRY(cudaSetDevice(eng->device));
+    order_quiesce(eng);
     GSS_TRY(train_finish(eng, true));
     GSS_TRY(train_start(eng));
     return train_finish(eng, true);
@@ -1097,12 +1233,16 @@ int gss_order_clause_features(gss_engine *eng, const uint32_t *ids, int64_t n, f
     if (n == 0) return GSS_OK;
     OrderState &o = *eng->order;
     GSS_CUDA_TRY(cudaSetDevice(eng->device));
+    order_quiesce(eng);
     const int64_t n_rec = std::min<int64_t>(eng->next_id, o.cap_ids);
     // a host copy of the records (a diagnostic, not a hot path)
     std::vector<ClauseRecord> rec((size_t) n_rec);
     if (n_rec) GSS_CUDA_TRY(cudaMemcpy(rec.data(), o.rec.ptr, n_rec * sizeof(ClauseRecord), cudaMemcpyDeviceToHost));
-    // features of the next pass: the counts of the last pass folded in
-    const int32_t now = (int32_t) o.pass;
+    // features of the next pass q: now = q - 1, and the counts of pass q - 2
+    // folded in (already done when the next pass was scored in advance)
+    const int64_t q = o.pass;
+    const int32_t now = (int32_t) (q - 1);
+    const bool fold = o.folded_pass < q && q >= 2;
     for (int64_t i = 0; i < n; i++) {
         const uint32_t id = ids[i];
         if (id >= eng->next_id || eng->index_of.size() <= id || eng->index_of[id] == 0xFFFFFFFFu ||
@@ -1113,10 +1253,16 @@ int gss_order_clause_features(gss_engine *eng, const uint32_t *ids, int64_t n, f
         const ClauseRecord &r = rec[id];
         float f[kF];
         if (id < o.known_ids) {
-            const uint32_t c = r.cur;
-            const uint64_t hh = (r.hist << 8) | (uint64_t) std::min<uint32_t>(c, 255u);
-            const int32_t lst = c ? now - 1 : r.last;
-            clause_features(len, r.lbd, now - r.birth, hh, r.total + c, lst < 0 ? -1 : now - lst, f);
+            uint64_t hh = r.hist;
+            uint32_t tot = r.total;
+            int32_t lst = r.last;
+            if (fold) {
+                const uint32_t c = (q & 1) ? r.cur1 : r.cur0;
+                hh = (hh << 8) | (uint64_t) std::min<uint32_t>(c, 255u);
+                tot += c;
+                if (c) lst = (int32_t) (q - 2);
+            }
+            clause_features(len, r.lbd, now - r.birth, hh, tot, lst < 0 ? -1 : now - lst, f);
         } else {
             clause_features(len, r.lbd, 0, 0, 0, -1, f);  // first scored in the next pass
         }
@@ -1140,6 +1286,7 @@ int gss_order_set_weights(gss_engine *eng, const float *w) {
     if (!eng->order) return set_error(GSS_ERR_STATE, "the learned order is not enabled");
     if (eng->pass_pending) return set_error(GSS_ERR_STATE, "a pass is in flight");
     GSS_CUDA_TRY(cudaSetDevice(eng->device));
+    order_quiesce(eng);
     GSS_TRY(train_finish(eng, true));
     GSS_CUDA_TRY(cudaMemcpyAsync(eng->order->scorer.w.ptr, w, kP * sizeof(float), cudaMemcpyHostToDevice,
                                  eng->stream));

@@ -227,7 +227,9 @@ int gss_check_noalloc(const int32_t *lits, const int64_t *offsets, uint32_t n_cl
  * whose reports gss_check_wait_head returns while the tail still runs, and
  * the tail. Every clause is still checked: the report set of a pass is the
  * plain scan's. Weights are FP32; inference runs the two matrix layers on
- * tensor cores with BF16 operands and FP32 accumulation. Training uses a log
+ * tensor cores with BF16 operands and FP32 accumulation. The order of the
+ * next pass is computed on a stream of its own while the tail of the current
+ * pass runs, so it sees reports up to two passes back. Training uses a log
  * of (features, reported) rows sampled from past passes: every
  * retrain_interval passes, train_epochs epochs of Adam on minibatches.
  * The learned order runs the direct and wide kernels through
@@ -242,6 +244,8 @@ typedef struct gss_order_params {
     int64_t log_capacity;      /* logged rows kept, newest first (default 2^20) */
     double log_rate;           /* share of clauses logged per pass (0 = about 2000 rows a pass) */
     uint64_t seed;             /* weight initialisation and minibatch sampling */
+    int overlap;               /* 1: the next pass is scored while this pass's tail runs (default);
+                                  0: once this pass has ended */
 } gss_order_params;
 
 void gss_order_params_default(gss_order_params *p);
@@ -257,6 +261,9 @@ int gss_db_set_lbd(gss_engine *eng, const uint32_t *ids, const uint16_t *lbd, in
 /* Waits for the head launch of the pass in flight and copies its reports
  * (they are also among the pass's reports from gss_check_copy_reports). */
 int gss_check_wait_head(gss_engine *eng, gss_report *out, int64_t cap, int64_t *n_reports);
+/* After gss_check_wait_head: waits for the pass and copies only the reports
+ * that were not in its head (head + tail = the pass's reports). */
+int gss_check_copy_tail(gss_engine *eng, gss_report *out, int64_t cap, int64_t *n_reports);
 typedef struct gss_order_stats {
     int64_t passes;            /* ordered passes so far */
     int64_t trainings;

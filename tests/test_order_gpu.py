@@ -108,7 +108,11 @@ def test_ordered_pass_reports_equal_plain(lib):
         eng.set_capacity(1 << 20)
         eng.launch()
         head = eng.wait_head()
-        ordered = eng.reports()
+        if p % 2:
+            ordered = eng.reports()
+        else:  # head + tail is the pass
+            ordered = np.concatenate([head, eng.copy_tail()])
+            assert len(ordered) == len(eng.reports())
         eng.order_set_active(False)
         plain = eng.check()
         eng.order_set_active(True)
@@ -130,8 +134,12 @@ def test_order_features_follow_the_report_history(lib):
     lbd = rng.integers(1, 20, size=ids.shape[0]).astype(np.uint16)
     eng.set_lbd(ids, lbd)
     lbd_of = {int(i): int(b) for i, b in zip(ids, lbd)}
+    # The scoring of pass q sees the reports of passes up to q-2 (pass q-1
+    # may still run while pass q is ordered) and uses now = q-1; the first
+    # scoring (q = 0) records births at now = -1.
     h = mlp.History()
-    h.born(range(n), 0)
+    h.born(range(n), -1)
+    per_pass = []
     for p in range(11):
         start = rng.integers(0, 2 ** 32, size=wl.n_words, dtype=np.uint32)
         eng.set_state(wl.state, start, wl.solver_of_word)
@@ -139,10 +147,12 @@ def test_order_features_follow_the_report_history(lib):
         counts = {}
         for c, m in zip(rep["clause"].tolist(), rep["mask"].tolist()):
             counts[c] = counts.get(c, 0) + bin(m).count("1")
-        h.record(p, counts)
+        per_pass.append(counts)
+    for p in range(10):
+        h.record(p, per_pass[p])
     sample = ids[:400]
     got = eng.order_features(sample)
-    want = np.stack([h.features(int(i), int(lens[i]), lbd_of[int(i)], 11) for i in sample])
+    want = np.stack([h.features(int(i), int(lens[i]), lbd_of[int(i)], 10) for i in sample])
     assert np.allclose(got, want, rtol=1e-6, atol=1e-6)
     eng.close()
 
