@@ -1,15 +1,24 @@
 // Logging helpers the sharer's callers use (the reference's
 // gpuShareLib/Utils.h:128-154): a Logger with a verbosity and an output
 // function, the LOG macro, directPrint and a wall clock in microseconds.
+// The solvers also rely on what this header brings in (the reference's
+// gpuShareLib/Utils.h:22-30): the assertion macros and <mutex>, <atomic>,
+// <memory> and <time.h>.
 #ifndef GPUSHARESAT_GB300_UTILS_H
 #define GPUSHARESAT_GB300_UTILS_H
 
 #include <sys/time.h>
+#include <time.h>
 
+#include <atomic>
 #include <functional>
 #include <iostream>
+#include <memory>
+#include <mutex>
 #include <sstream>
 #include <string>
+
+#include "Assert.h"
 
 namespace GpuShare {
 
