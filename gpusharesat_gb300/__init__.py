@@ -101,6 +101,7 @@ def load():
     _sig(lib, "gss_order_get_stats", c_int, vp, vp)
     _sig(lib, "gss_order_train", c_int, vp)
     _sig(lib, "gss_order_clause_features", c_int, vp, vp, c_i64, vp)
+    _sig(lib, "gss_order_scan_ranks", c_int, vp, vp, c_i64, vp)
     _sig(lib, "gss_order_get_weights", c_int, vp, vp)
     _sig(lib, "gss_order_set_weights", c_int, vp, vp)
     _sig(lib, "gss_scorer_create", c_int, c_int, ctypes.c_uint64, vp)
@@ -328,6 +329,13 @@ class Engine:
         x = np.zeros((ids.shape[0], SCORER_FEATURES), dtype=np.float32)
         _check(self.lib.gss_order_clause_features(self.h, _ptr(ids), ids.shape[0], _ptr(x)))
         return x
+
+    def scan_ranks(self, ids):
+        """Rank of each clause id in the last ordered pass's scan (-1: absent)."""
+        ids = np.ascontiguousarray(ids, dtype=np.uint32)
+        out = np.zeros(ids.shape[0], dtype=np.int64)
+        _check(self.lib.gss_order_scan_ranks(self.h, _ptr(ids), ids.shape[0], _ptr(out)))
+        return out
 
     def order_weights(self):
         w = np.zeros(SCORER_PARAMS, dtype=np.float32)

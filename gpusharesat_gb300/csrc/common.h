@@ -90,9 +90,11 @@ struct CheckArgs {
     const uint32_t *alive;        // device, 1 bit per clause (NULL: every clause is live)
     uint32_t alive_by_id;         // alive is indexed by orig[c] rather than by c
     // Scan order: this launch checks the clauses at scan positions
-    // [scan_begin, scan_end); position i is clause perm[i] (NULL: clause i).
+    // [scan_begin, scan_end); position i is clause perm[i] when perm is set
+    // and i < perm_end, clause i otherwise.
     const uint32_t *perm;
     uint32_t scan_begin, scan_end;
+    uint32_t perm_end;
 };
 
 __host__ __device__ __forceinline__ uint32_t scan_count(const CheckArgs &a) {
@@ -100,7 +102,8 @@ __host__ __device__ __forceinline__ uint32_t scan_count(const CheckArgs &a) {
 }
 // Clause at offset i of this launch's scan range (i < scan_count).
 __device__ __forceinline__ uint32_t scan_clause(const CheckArgs &a, uint32_t i) {
-    return a.perm ? __ldg(a.perm + a.scan_begin + i) : a.scan_begin + i;
+    const uint32_t p = a.scan_begin + i;
+    return (a.perm && p < a.perm_end) ? __ldg(a.perm + p) : p;
 }
 
 // Whether clause c of the database takes part in the pass.

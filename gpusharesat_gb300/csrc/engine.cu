@@ -761,19 +761,16 @@ int launch_pass_into(gss_engine *eng, const void *state, DevBuf &reports, DevBuf
         // counts for early delivery, the tail, and the history update
         uint32_t head = 0, covered = 0;
         GSS_TRY(order_prepare(eng, &a.perm, &head, &covered));
+        // positions appended since the order was computed (from `covered`
+        // on) are scanned in place at the end of the tail
+        a.perm_end = covered;
         a.scan_begin = 0;
         a.scan_end = head;
         if (head) GSS_TRY(launch(a));
         GSS_TRY(order_after_head(eng, counts));
         a.scan_begin = head;
-        a.scan_end = covered;
-        if (head < covered) GSS_TRY(launch(a));
-        if (covered < a.n_clauses) {  // appended since the order was computed
-            a.perm = nullptr;
-            a.scan_begin = covered;
-            a.scan_end = a.n_clauses;
-            GSS_TRY(launch(a));
-        }
+        a.scan_end = a.n_clauses;
+        if (head < a.n_clauses) GSS_TRY(launch(a));
         GSS_TRY(order_after_pass(eng, reports, counts));
     } else {
         GSS_TRY(launch(a));

@@ -10,12 +10,13 @@
 //      (features, reported) rows for training, computes the features, runs
 //      the MLP on tensor cores (mma.sync m16n8k16, BF16 operands, FP32
 //      accumulation) and writes the clause's score bucket
-//   3. bucket_hist_kernel, bucket_scan_kernel, bucket_base_kernel,
-//      bucket_scatter_kernel: a stable
-//      one-digit radix sort of positions by score bucket. The plain position
-//      order is sorted by length, so within a bucket the scan stays in length
-//      order (lane groups of a warp keep clauses of one length, as in the
-//      plain scan)
+//   3. bucket_hist_kernel, bucket_scan_kernel, head_key_kernel, then a
+//      stable one-digit radix sort of positions (bucket_hist, bucket_scan,
+//      bucket_base, bucket_scatter) by key: the score bucket for the clauses
+//      of the head (the best buckets up to head_fraction of the clauses), one
+//      key for the tail. The plain position order is sorted by length, so a
+//      head bucket stays in length order (lane groups of a warp keep clauses
+//      of one length), and the tail keeps the plain order and its locality
 // After the pass (order_after_pass): history_kernel adds each report's slot
 // count to its clause's counter for the pass, and the scoring of the next
 // pass is enqueued on a stream of its own, behind the head of this pass: it
@@ -505,7 +506,7 @@ struct OrderState {
     int64_t cap_ids = 0;
     DevBuf rec;                                 // ClauseRecord per clause id
     DevBuf lbd_pairs;                           // staging of gss_db_set_lbd
-    DevBuf bucket, offs, totals;                // per position; per (bucket, sort tile); per bucket
+    DevBuf bucket, offs, totals, key_of;        // per position; per (bucket, sort tile); per bucket (x2)
     DevBuf perm[2];                             // scan permutation of passes with even / odd numbers
     // the order of the next pass, computed on score_stream while the tail of
     // the current pass runs (pre_*: what it was computed for)
@@ -682,6 +683,29 @@ __device__ uint32_t block_scan_inplace(uint32_t *__restrict__ a, uint32_t n) {
     return carry;
 }
 
+// The sort key of each score bucket for the final order: the bucket itself
+// while the clauses of better buckets number fewer than `cut` (the head,
+// ordered by score), kBuckets - 2 for the rest (the tail, which then keeps
+// the plain position order and its memory locality), kBuckets - 1 for
+// deleted clauses. totals holds the clause count of each bucket. One block
+// of kBuckets threads.
+__global__ void head_key_kernel(const uint32_t *__restrict__ totals, uint32_t cut, uint8_t *__restrict__ key_of) {
+    __shared__ uint32_t before[kBuckets];
+    const int b = threadIdx.x;
+    before[b] = totals[b];
+    __syncthreads();
+    if (b == 0) {
+        uint32_t acc = 0;
+        for (int k = 0; k < kBuckets; k++) {
+            const uint32_t c = before[k];
+            before[k] = acc;
+            acc += c;
+        }
+    }
+    __syncthreads();
+    key_of[b] = (uint8_t) (b == kBuckets - 1 ? kBuckets - 1 : before[b] < cut ? b : kBuckets - 2);
+}
+
 // Block b: exclusive scan of bucket b's per-tile counts; totals[b] = its sum.
 __global__ void bucket_scan_kernel(uint32_t *__restrict__ offs, uint32_t n_tiles, uint32_t *__restrict__ totals) {
     const uint32_t t = block_scan_inplace(offs + (size_t) blockIdx.x * n_tiles, n_tiles);
@@ -694,7 +718,8 @@ __global__ void bucket_base_kernel(uint32_t *__restrict__ totals, uint32_t n) { 
 
 // Per sort tile: how many positions fall in each bucket, stored bucket-major
 // (offs[b * n_tiles + tile]) for the scan.
-__global__ void __launch_bounds__(kSortThreads) bucket_hist_kernel(const uint8_t *__restrict__ bucket, uint32_t n,
+__global__ void __launch_bounds__(kSortThreads) bucket_hist_kernel(const uint8_t *__restrict__ bucket,
+                                                                   const uint8_t *__restrict__ key_of, uint32_t n,
                                                                    uint32_t n_tiles, uint32_t *__restrict__ offs) {
     __shared__ uint32_t hist[kBuckets];
     hist[threadIdx.x] = 0;
@@ -702,7 +727,7 @@ __global__ void __launch_bounds__(kSortThreads) bucket_hist_kernel(const uint8_t
     const uint32_t base = blockIdx.x * kSortTile;
     for (int r = 0; r < kSortRounds; r++) {
         const uint32_t pos = base + r * kSortThreads + threadIdx.x;
-        if (pos < n) atomicAdd(&hist[bucket[pos]], 1u);
+        if (pos < n) atomicAdd(&hist[key_of ? key_of[bucket[pos]] : bucket[pos]], 1u);
     }
     __syncthreads();
     offs[(size_t) threadIdx.x * n_tiles + blockIdx.x] = hist[threadIdx.x];
@@ -711,7 +736,8 @@ __global__ void __launch_bounds__(kSortThreads) bucket_hist_kernel(const uint8_t
 // Stable scatter: positions of a bucket keep their order. Each round takes
 // kSortThreads consecutive positions; a position's rank is its rank among the
 // equal buckets of its warp (match) plus the counts of the earlier warps.
-__global__ void __launch_bounds__(kSortThreads) bucket_scatter_kernel(const uint8_t *__restrict__ bucket, uint32_t n,
+__global__ void __launch_bounds__(kSortThreads) bucket_scatter_kernel(const uint8_t *__restrict__ bucket,
+                                                                      const uint8_t *__restrict__ key_of, uint32_t n,
                                                                       uint32_t n_tiles,
                                                                       const uint32_t *__restrict__ offs,
                                                                       const uint32_t *__restrict__ base_of,
@@ -728,7 +754,7 @@ __global__ void __launch_bounds__(kSortThreads) bucket_scatter_kernel(const uint
         __syncthreads();
         const uint32_t pos = base + r * kSortThreads + threadIdx.x;
         const bool valid = pos < n;
-        const uint32_t b = valid ? bucket[pos] : (uint32_t) kBuckets;  // kBuckets: no position
+        const uint32_t b = valid ? (key_of ? key_of[bucket[pos]] : bucket[pos]) : (uint32_t) kBuckets;  // kBuckets: none
         const unsigned peers = __match_any_sync(kFullMask, b);
         const unsigned lt = (1u << lane) - 1u;
         const uint32_t rank = (uint32_t) __popc(peers & lt);
@@ -891,6 +917,14 @@ void order_quiesce(gss_engine *eng) {
 
 namespace {
 
+// Scan positions in the head of a pass over n clauses.
+uint32_t head_cut(const OrderState &o, uint32_t n) {
+    double hf = o.prm.head_fraction;
+    if (!(hf > 0.0)) hf = 0.0;
+    if (hf > 1.0) hf = 1.0;
+    return (uint32_t) std::min<double>((double) n, ceil(hf * (double) n));
+}
+
 // Enqueues on `st` the scoring and ordering of pass q over the database as it
 // is now, into perm[q & 1]; returns the positions covered.
 int score_pass(gss_engine *eng, cudaStream_t st, int64_t q, uint32_t *covered) {
@@ -919,6 +953,7 @@ int score_pass(gss_engine *eng, cudaStream_t st, int64_t q, uint32_t *covered) {
     GSS_TRY(o.bucket.reserve(std::max<size_t>(n, 1)));
     GSS_TRY(o.offs.reserve(std::max<size_t>((size_t) kBuckets * n_tiles, 1) * sizeof(uint32_t)));
     GSS_TRY(o.totals.reserve(kBuckets * sizeof(uint32_t)));
+    GSS_TRY(o.key_of.reserve(kBuckets));
     if (n) {
         // history fold, training log, features, MLP, score bucket
         score_kernel<<<grid_for_n((uint64_t) (n + 31) / 32 * 32, eng->sm_count, kMlpThreads), kMlpThreads, 0, st>>>(
@@ -926,15 +961,27 @@ int score_pass(gss_engine *eng, cudaStream_t st, int64_t q, uint32_t *covered) {
             (const int64_t *) eng->offsets.ptr, (const uint32_t *) eng->orig.ptr,
             eng->n_dead > 0 ? (const uint32_t *) eng->alive.ptr : nullptr, n, (uint8_t *) o.bucket.ptr);
         GSS_CUDA_TRY(cudaGetLastError());
-        // stable radix sort of positions by bucket
-        bucket_hist_kernel<<<n_tiles, kSortThreads, 0, st>>>((const uint8_t *) o.bucket.ptr, n, n_tiles,
+        // the clauses per score bucket, then the sort key of each bucket:
+        // score order in the head, plain order in the tail
+        bucket_hist_kernel<<<n_tiles, kSortThreads, 0, st>>>((const uint8_t *) o.bucket.ptr, nullptr, n, n_tiles,
+                                                              (uint32_t *) o.offs.ptr);
+        GSS_CUDA_TRY(cudaGetLastError());
+        bucket_scan_kernel<<<kBuckets, 1024, 0, st>>>((uint32_t *) o.offs.ptr, n_tiles, (uint32_t *) o.totals.ptr);
+        GSS_CUDA_TRY(cudaGetLastError());
+        head_key_kernel<<<1, kBuckets, 0, st>>>((const uint32_t *) o.totals.ptr, head_cut(o, n),
+                                                (uint8_t *) o.key_of.ptr);
+        GSS_CUDA_TRY(cudaGetLastError());
+        // stable radix sort of positions by key
+        bucket_hist_kernel<<<n_tiles, kSortThreads, 0, st>>>((const uint8_t *) o.bucket.ptr,
+                                                              (const uint8_t *) o.key_of.ptr, n, n_tiles,
                                                               (uint32_t *) o.offs.ptr);
         GSS_CUDA_TRY(cudaGetLastError());
         bucket_scan_kernel<<<kBuckets, 1024, 0, st>>>((uint32_t *) o.offs.ptr, n_tiles, (uint32_t *) o.totals.ptr);
         GSS_CUDA_TRY(cudaGetLastError());
         bucket_base_kernel<<<1, kBuckets, 0, st>>>((uint32_t *) o.totals.ptr, kBuckets);
         GSS_CUDA_TRY(cudaGetLastError());
-        bucket_scatter_kernel<<<n_tiles, kSortThreads, 0, st>>>((const uint8_t *) o.bucket.ptr, n, n_tiles,
+        bucket_scatter_kernel<<<n_tiles, kSortThreads, 0, st>>>((const uint8_t *) o.bucket.ptr,
+                                                                 (const uint8_t *) o.key_of.ptr, n, n_tiles,
                                                                  (const uint32_t *) o.offs.ptr,
                                                                  (const uint32_t *) o.totals.ptr,
                                                                  (uint32_t *) perm.ptr);
@@ -972,10 +1019,7 @@ int order_prepare(gss_engine *eng, const uint32_t **perm, uint32_t *head, uint32
     }
     o.pre_ready = false;
     o.pass = q + 1;
-    double hf = o.prm.head_fraction;
-    if (!(hf > 0.0)) hf = 0.0;
-    if (hf > 1.0) hf = 1.0;
-    o.head = (uint32_t) std::min<double>((double) n_scored, ceil(hf * (double) n_scored));
+    o.head = head_cut(o, n_scored);
     o.scored_n = n_scored;
     *perm = (const uint32_t *) o.perm[q & 1].ptr;
     *head = o.head;
@@ -1185,6 +1229,31 @@ int gss_check_copy_tail(gss_engine *eng, gss_report *out, int64_t cap, int64_t *
         pos += ac[q] - hc[q];
     }
     GSS_CUDA_TRY(cudaStreamSynchronize(eng->stream));
+    return GSS_OK;
+}
+
+int gss_order_scan_ranks(gss_engine *eng, const uint32_t *ids, int64_t n, int64_t *ranks) {
+    if (!eng || n < 0 || (n > 0 && (!ids || !ranks))) return set_error(GSS_ERR_INVALID, "bad arguments");
+    if (!eng->order || eng->order->pass == 0) return set_error(GSS_ERR_STATE, "no ordered pass yet");
+    if (n == 0) return GSS_OK;
+    OrderState &o = *eng->order;
+    GSS_CUDA_TRY(cudaSetDevice(eng->device));
+    GSS_CUDA_TRY(cudaStreamSynchronize(eng->stream));
+    // the last pass's permutation, inverted on the host (a diagnostic)
+    const uint32_t covered = o.scored_n;
+    std::vector<uint32_t> perm(covered);
+    if (covered)
+        GSS_CUDA_TRY(cudaMemcpy(perm.data(), o.perm[(o.pass - 1) & 1].ptr, covered * sizeof(uint32_t),
+                                cudaMemcpyDeviceToHost));
+    std::vector<int64_t> rank_of_pos((size_t) eng->n_clauses, -1);
+    for (uint32_t r = 0; r < covered; r++)
+        if (perm[r] < rank_of_pos.size()) rank_of_pos[perm[r]] = r;
+    for (int64_t p = covered; p < eng->n_clauses; p++) rank_of_pos[p] = p;  // scanned in place
+    for (int64_t i = 0; i < n; i++) {
+        const uint32_t id = ids[i];
+        const uint32_t pos = id < eng->index_of.size() ? eng->index_of[id] : 0xFFFFFFFFu;
+        ranks[i] = pos == 0xFFFFFFFFu || pos >= rank_of_pos.size() ? -1 : rank_of_pos[pos];
+    }
     return GSS_OK;
 }
 

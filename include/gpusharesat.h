@@ -278,6 +278,10 @@ int gss_order_get_stats(gss_engine *eng, gss_order_stats *out);
 int gss_order_train(gss_engine *eng);
 /* Features the next pass will score the given clauses with, x[n][12]. */
 int gss_order_clause_features(gss_engine *eng, const uint32_t *ids, int64_t n, float *x);
+/* Rank of each clause id in the last ordered pass's scan (0 = scanned
+ * first; -1 = not in the database). A diagnostic: it copies and inverts the
+ * permutation on the host. */
+int gss_order_scan_ranks(gss_engine *eng, const uint32_t *ids, int64_t n, int64_t *ranks);
 /* The order's MLP weights (GSS_SCORER_PARAMS floats, layout as below). */
 int gss_order_get_weights(gss_engine *eng, float *w);
 int gss_order_set_weights(gss_engine *eng, const float *w);

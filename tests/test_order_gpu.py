@@ -120,6 +120,10 @@ def test_ordered_pass_reports_equal_plain(lib):
         assert key(ordered) == key(plain)
         assert key(head) <= key(plain)
         assert len(plain) > 0
+        # the scan ranks are a permutation, and the head's clauses rank first
+        ranks = eng.scan_ranks(np.arange(wl.n_clauses, dtype=np.uint32))
+        assert np.array_equal(np.sort(ranks), np.arange(wl.n_clauses))
+        assert np.all(eng.scan_ranks(head["clause"]) < 2000)
     st = eng.order_stats()
     assert st["passes"] == 4 and st["head_positions"] == 2000
     eng.close()
