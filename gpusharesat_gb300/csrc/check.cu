@@ -91,15 +91,23 @@ __device__ __forceinline__ int32_t ld_lit(const int32_t *p, bool hint, uint64_t 
     return v;
 }
 
+// Writes a warp's staged records: one atomic reservation, then the records.
+// streaming = cache-streaming stores (the records are read back by the host,
+// not by the kernel: they need not displace state rows from L2).
 __device__ __forceinline__ void flush_stage(gss_report *stage, uint32_t n, gss_report *out, uint32_t *counter,
-                                            uint32_t cap, int lane) {
+                                            uint32_t cap, int lane, bool streaming = false) {
     __syncwarp();
     uint32_t base = 0;
     if (lane == 0) base = atomicAdd(counter, n);
     base = __shfl_sync(kFull, base, 0);
     for (uint32_t i = lane; i < n; i += 32) {
         uint32_t idx = base + i;
-        if (idx < cap) out[idx] = stage[i];
+        if (idx < cap) {
+            if (streaming)
+                __stcs(reinterpret_cast<int4 *>(out + idx), *reinterpret_cast<const int4 *>(stage + i));
+            else
+                out[idx] = stage[i];
+        }
     }
     __syncwarp();
 }
@@ -240,8 +248,31 @@ __device__ __forceinline__ void ld_row<4>(const uint2 *p, Row<4> &r) {
         : "l"(p));
 }
 
+// The same gathers with an L2 eviction policy (cache_hints on).
+template <int WPL>
+__device__ __forceinline__ void ld_row_hint(const uint2 *p, Row<WPL> &r, uint64_t pol);
+template <>
+__device__ __forceinline__ void ld_row_hint<1>(const uint2 *p, Row<1> &r, uint64_t pol) {
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.v2.u32 {%0, %1}, [%2], %3;"
+        : "=r"(r.v[0]), "=r"(r.v[1]) : "l"(p), "l"(pol));
+}
+template <>
+__device__ __forceinline__ void ld_row_hint<2>(const uint2 *p, Row<2> &r, uint64_t pol) {
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
+        : "=r"(r.v[0]), "=r"(r.v[1]), "=r"(r.v[2]), "=r"(r.v[3]) : "l"(p), "l"(pol));
+}
+template <>
+__device__ __forceinline__ void ld_row_hint<4>(const uint2 *p, Row<4> &r, uint64_t pol) {
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.v8.u32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8], %9;"
+        : "=r"(r.v[0]), "=r"(r.v[1]), "=r"(r.v[2]), "=r"(r.v[3]), "=r"(r.v[4]), "=r"(r.v[5]), "=r"(r.v[6]),
+          "=r"(r.v[7])
+        : "l"(p), "l"(pol));
+}
+
 // MAP_IDS = false: reports carry the clause's CSR index itself (a.orig unused).
-template <int WPL, int LPC, int G, int MINB, bool MAP_IDS = true>
+// With cache_hints: state rows evict-last in L2, clause literals evict-first,
+// report records streamed.
+template <int WPL, int LPC, int G, int MINB, bool MAP_IDS = true, bool HINT = false>
 __global__ void __launch_bounds__(kWarps * 32, MINB) check_wide_kernel(CheckArgs a) {
     constexpr int CPW = 32 / LPC;
     constexpr int BW = WPL * LPC;
@@ -257,6 +288,9 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) check_wide_kernel(CheckArgs
     gss_report *out = a.out + (size_t) part * a.cap_per_part;
     uint32_t *counter = a.counts + part;
     uint32_t nstaged = 0;
+    constexpr bool hint = HINT;
+    const uint64_t pol_keep = hint ? policy_evict_last() : 0ull;
+    const uint64_t pol_stream = hint ? policy_evict_first() : 0ull;
 
     const uint32_t n_scan = scan_count(a);
     const uint32_t n_groups = (n_scan + CPW - 1) / CPW;
@@ -286,7 +320,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) check_wide_kernel(CheckArgs
 #pragma unroll
             for (int j = 0; j < WPL; j++) alive |= (af[j] | ou[j]) != 0u;
             if (!__any_sync(kFull, alive && pos < end)) break;
-            const int32_t chunk = (pos + sub < end) ? __ldg(a.lits + pos + sub) : 0;
+            const int32_t chunk = (pos + sub < end) ? ld_lit(a.lits + pos + sub, hint, pol_stream) : 0;
             const int navail = (int) min((uint32_t) LPC, end > pos ? end - pos : 0u);
 #pragma unroll 1
             for (int k0 = 0; k0 < LPC; k0 += G) {
@@ -302,7 +336,12 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) check_wide_kernel(CheckArgs
                 for (int i = 0; i < G; i++) {
 #pragma unroll
                     for (int q = 0; q < 2 * WPL; q++) st[i].v[q] = 0u;
-                    if (alive && k0 + i < navail) ld_row<WPL>(rows + (size_t) (lit[i] >> 1) * BW, st[i]);
+                    if (alive && k0 + i < navail) {
+                        if (hint)
+                            ld_row_hint<WPL>(rows + (size_t) (lit[i] >> 1) * BW, st[i], pol_keep);
+                        else
+                            ld_row<WPL>(rows + (size_t) (lit[i] >> 1) * BW, st[i]);
+                    }
                 }
 #pragma unroll
                 for (int i = 0; i < G; i++) {
@@ -326,7 +365,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) check_wide_kernel(CheckArgs
             const unsigned bal = __ballot_sync(kFull, rep != 0u);
             if (bal) {
                 if (nstaged + 32 > (uint32_t) kStage) {
-                    flush_stage(stage, nstaged, out, counter, a.cap_per_part, lane);
+                    flush_stage(stage, nstaged, out, counter, a.cap_per_part, lane, hint);
                     nstaged = 0;
                 }
                 if (rep) {
@@ -341,7 +380,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) check_wide_kernel(CheckArgs
             }
         }
     }
-    if (nstaged) flush_stage(stage, nstaged, out, counter, a.cap_per_part, lane);
+    if (nstaged) flush_stage(stage, nstaged, out, counter, a.cap_per_part, lane, hint);
 }
 
 // Pipelined wide variant: the same schedule and rule as check_wide_kernel,
@@ -631,11 +670,11 @@ int launch_wide_pf_variant(const CheckArgs &a, cudaStream_t stream, int sm_count
     return GSS_OK;
 }
 
-template <int WPL, int LPC, int G, int MINB, bool MAP_IDS = true>
+template <int WPL, int LPC, int G, int MINB, bool MAP_IDS = true, bool HINT = false>
 int launch_wide_variant(const CheckArgs &a, cudaStream_t stream, int sm_count) {
     int per_sm = 0;
-    GSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, check_wide_kernel<WPL, LPC, G, MINB, MAP_IDS>,
-                                                               kWarps * 32, 0));
+    GSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm, check_wide_kernel<WPL, LPC, G, MINB, MAP_IDS, HINT>, kWarps * 32, 0));
     if (per_sm < 1) per_sm = 1;
     constexpr int CPW = 32 / LPC;
     const uint64_t n_tasks = (uint64_t) ((scan_count(a) + CPW - 1) / CPW) * a.n_blocks;
@@ -643,7 +682,7 @@ int launch_wide_variant(const CheckArgs &a, cudaStream_t stream, int sm_count) {
     const uint64_t need = (n_tasks + kWarps - 1) / kWarps;
     if (blocks > need) blocks = need;
     if (blocks < 1) blocks = 1;
-    check_wide_kernel<WPL, LPC, G, MINB, MAP_IDS><<<(unsigned) blocks, kWarps * 32, 0, stream>>>(a);
+    check_wide_kernel<WPL, LPC, G, MINB, MAP_IDS, HINT><<<(unsigned) blocks, kWarps * 32, 0, stream>>>(a);
     GSS_CUDA_TRY(cudaGetLastError());
     return GSS_OK;
 }
@@ -736,6 +775,12 @@ bool valid_wide_pf_variant(int wpl, int lpc, int g) {
 
 int launch_check_wide(const CheckArgs &a, int wpl, int occ, cudaStream_t stream, int sm_count) {
     if (a.n_clauses == 0 || a.n_blocks == 0 || scan_count(a) == 0) return GSS_OK;
+    // L2 policies (cache_hints) for the 4-words-per-lane, 8-lane kinds
+    if (wpl == 4 && a.lpc == 8 && !occ && a.cache_hints) {
+        if (a.g == 1) return launch_wide_variant<4, 8, 1, 1, true, true>(a, stream, sm_count);
+        if (a.g == 2) return launch_wide_variant<4, 8, 2, 1, true, true>(a, stream, sm_count);
+        if (a.g == 4) return launch_wide_variant<4, 8, 4, 1, true, true>(a, stream, sm_count);
+    }
 #define GSS_WV(W, L, GG)                                                                      \
     if (wpl == W && a.lpc == L && a.g == GG)                                                  \
         return occ ? launch_wide_variant<W, L, GG, 8>(a, stream, sm_count)                    \
