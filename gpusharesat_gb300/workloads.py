@@ -306,3 +306,50 @@ def make_learned(seed=4, n_vars=2 ** 21, n_clauses=4_000_000, n_words=64, stream
     state[:, :, 1] = np.where(model[:, None] == 1, np.uint32(0xFFFFFFFF), np.uint32(0))
     return {"lits": lits, "offsets": offsets, "rate": r, "lbd": lbd, "state": state, "model": model,
             "n_vars": n_vars, "n_words": n_words, "n_clauses": n_clauses, "stream": stream}
+
+
+# ---- dump format shared by the harnesses ----
+#
+# One .npz file per workload: the arrays of Workload (lits, offsets, state,
+# start, solver_of_word, planted) plus its name, variable count and solver
+# count. The oracle, the engine, bench.py and the tests can all load it.
+
+def save(wl, path):
+    """Writes a Workload to `path` (.npz)."""
+    np.savez(path, name=np.array(wl.name), n_vars=np.int64(wl.n_vars), n_solvers=np.int64(wl.n_solvers),
+             lits=wl.lits, offsets=wl.offsets, state=wl.state, start=wl.start,
+             solver_of_word=wl.solver_of_word, planted=wl.planted)
+
+
+def load(path):
+    """Reads a Workload written by save()."""
+    with np.load(path, allow_pickle=False) as z:
+        return Workload(str(z["name"]), int(z["n_vars"]), z["lits"], z["offsets"], z["state"], z["start"],
+                        z["solver_of_word"], int(z["n_solvers"]), z["planted"])
+
+
+MAKERS = {"small": make_small, "scale": make_scale, "batching": make_batching}
+
+
+def main(argv=None):
+    """python -m gpusharesat_gb300.workloads {small|scale|batching} OUT.npz [--clauses N] [--seed S]"""
+    import argparse
+    p = argparse.ArgumentParser()
+    p.add_argument("workload", choices=sorted(MAKERS))
+    p.add_argument("out")
+    p.add_argument("--clauses", type=int, default=None)
+    p.add_argument("--seed", type=int, default=None)
+    args = p.parse_args(argv)
+    kw = {}
+    if args.clauses is not None:
+        kw["n_clauses"] = args.clauses
+    if args.seed is not None:
+        kw["seed"] = args.seed
+    wl = MAKERS[args.workload](**kw)
+    save(wl, args.out)
+    print("%s: %d clauses, %d literals, %d variables, %d words -> %s"
+          % (wl.name, wl.n_clauses, wl.n_lits, wl.n_vars, wl.n_words, args.out))
+
+
+if __name__ == "__main__":
+    main()

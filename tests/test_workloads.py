@@ -24,3 +24,16 @@ def test_model_clauses_never_report_under_the_base_state(oracle_lib):
     assert np.all((d["lbd"] >= 1) & (d["lbd"] <= lens))
     hi = d["rate"] > np.quantile(d["rate"], 0.9)
     assert (d["lbd"][hi] / lens[hi]).mean() < (d["lbd"][~hi] / lens[~hi]).mean()
+
+
+def test_dump_round_trip(tmp_path, oracle_lib):
+    wl = W.make_small(seed=4, n_clauses=3000)
+    path = str(tmp_path / "small.npz")
+    W.save(wl, path)
+    back = W.load(path)
+    assert back.name == wl.name and back.n_vars == wl.n_vars and back.n_solvers == wl.n_solvers
+    for f in ("lits", "offsets", "state", "start", "solver_of_word", "planted"):
+        assert np.array_equal(getattr(back, f), getattr(wl, f)), f
+    a = oracle.check(wl.lits, wl.offsets, wl.state, wl.start)
+    b = oracle.check(back.lits, back.offsets, back.state, back.start)
+    assert np.array_equal(a, b)
