@@ -166,9 +166,10 @@ int gss_check_set_capacity(gss_engine *eng, int64_t records);
 /* Launches one pass over the whole database against the current state,
  * asynchronously on the engine's stream. */
 int gss_check_launch(gss_engine *eng);
-/* Waits for the last pass and returns its report count in *n_reports.
- * Returns GSS_ERR_OVERFLOW if the queues overflowed (nothing was lost for
- * good: raise the capacity and launch again). */
+/* Waits for the last pass and returns its report count in *n_reports (0 when
+ * no pass was launched yet). Returns GSS_ERR_OVERFLOW if the queues
+ * overflowed (nothing was lost for good: raise the capacity and launch
+ * again). */
 int gss_check_wait(gss_engine *eng, int64_t *n_reports);
 /* Copies the reports of the last pass to host memory `out` (capacity `cap`
  * records), in no particular order. */
@@ -222,10 +223,10 @@ int gss_check_noalloc(const int32_t *lits, const int64_t *offsets, uint32_t n_cl
  * A 12-64-64-1 MLP scores every clause before each pass from 12 features:
  * length, LBD, age, and the clause's report history (slot reports in each of
  * the last 8 passes, total reports, passes since the last report). The pass
- * then scans clauses in decreasing score, grouped by length within a score
- * bucket, as two launches: the head (the first head_fraction of the scan),
- * whose reports gss_check_wait_head returns while the tail still runs, and
- * the tail. Every clause is still checked: the report set of a pass is the
+ * then runs as two launches: the head, the first head_fraction of the scan
+ * in decreasing score (grouped by length within a score bucket), whose
+ * reports gss_check_wait_head returns while the tail still runs; and the
+ * tail, the other clauses in the plain order. Every clause is still checked: the report set of a pass is the
  * plain scan's. Weights are FP32; inference runs the two matrix layers on
  * tensor cores with BF16 operands and FP32 accumulation. The order of the
  * next pass is computed on a stream of its own while the tail of the current
