@@ -185,3 +185,21 @@ def test_serving_generator_short_run(lib):
     assert r["evicted"] > 0
     assert r["live_clauses_end"] <= 150_000
     assert r["reports_popped"] > 0
+
+
+def test_reduce_db_after_evictions(lib):
+    """A reduceDb on a database with evicted clauses drops the tombstones:
+    the clause count stays the live count, evicted clauses stay gone, and
+    the clauses it keeps still report."""
+    n_vars = 2000
+    s = make(n_vars, 2, budget=300)
+    for k in range(500):
+        s.addClause(-1, [lit(2 * k), lit(2 * k + 1)])  # binary: reduceDb keeps them all
+    assert s.trySetSolverValues(0, [lit(0)]) and s.trySendAssignment(0) >= 0
+    execute(s)
+    assert s.evictedCount() == 200 and s.getGlobalStat(GPU_CLAUSES) == 300
+    s.reduceDb()
+    assert s.getGlobalStat(GPU_CLAUSES) == 300
+    all_false(s, 1, n_vars)
+    execute(s)
+    assert popped_ids(s, 1) == list(range(200, 500))
