@@ -30,6 +30,15 @@ VARIANT_L2_HINT = 1
 VARIANT_OCCUPANCY = 2
 VARIANT_PIPELINED = 4
 VARIANT_PERSISTENT = 8
+# lane layouts of the bucketed kernel (Engine.set_length_plan)
+LAYOUT_SKIP = -1
+LAYOUT_4x8_G1 = 0
+LAYOUT_4x8_G2 = 1
+LAYOUT_2x16_G1 = 2
+LAYOUT_2x16_G2 = 3
+LAYOUT_1x32_G1 = 4
+LAYOUT_1x32_G2 = 5
+LAYOUTS = (LAYOUT_4x8_G1, LAYOUT_4x8_G2, LAYOUT_2x16_G1, LAYOUT_2x16_G2, LAYOUT_1x32_G1, LAYOUT_1x32_G2)
 
 REPORT_DTYPE = np.dtype([("clause", "<u4"), ("word", "<u4"), ("mask", "<u4"), ("solver", "<u4")])
 
@@ -91,6 +100,7 @@ def load():
     _sig(lib, "gss_check_pass_host", c_int, vp, vp, c_i64, c_int, vp, vp, vp, c_i64, vp)
     _sig(lib, "gss_check_passes_host", c_int, vp, c_int, vp, c_i64, c_int, vp, vp, vp, vp, vp)
     _sig(lib, "gss_db_positions", c_int, vp, vp, c_i64, vp)
+    _sig(lib, "gss_engine_set_length_plan", c_int, vp, c_int, vp, vp)
     _sig(lib, "gss_order_params_default", None, vp)
     _sig(lib, "gss_order_enable", c_int, vp, vp)
     _sig(lib, "gss_order_disable", c_int, vp)
@@ -257,6 +267,14 @@ class Engine:
                 _check(self.lib.gss_check_copy_reports(self.h, _ptr(out), out.shape[0], ctypes.byref(got)))
                 return out[:got.value]
         raise GssError(GSS_ERR_OVERFLOW, "report queues kept overflowing")
+
+    def set_length_plan(self, max_len=(), layouts=()):
+        """Per-length-class lane layouts in one persistent launch (the
+        bucketed kernel); empty turns the plan off."""
+        ml = np.ascontiguousarray(max_len, dtype=np.int32)
+        ly = np.ascontiguousarray(layouts, dtype=np.int32)
+        assert ml.shape == ly.shape
+        _check(self.lib.gss_engine_set_length_plan(self.h, ml.shape[0], _ptr(ml), _ptr(ly)))
 
     def positions(self, ids):
         """Position of each clause id in the plain scan order (-1: absent)."""

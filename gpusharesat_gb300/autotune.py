@@ -31,6 +31,54 @@ CANDIDATES_DIRECT = [(g.KERNEL_DIRECT, l, d, 0) for l, ds in ((1, (1,)), (2, (1,
 CANDIDATES_TILED = [(g.KERNEL_TILED, 0, k, 0) for k in (2, 4)]
 
 
+# length classes of the bucketed kernel: (1,4], (4,12], (12,32], (32,...)
+LENGTH_CLASSES = (4, 12, 32, 1 << 30)
+
+
+def tune_length_plan(engine, state, start, solver_of_word=None, classes=LENGTH_CLASSES, layouts=None, launches=4,
+                     warmup=1, log=None):
+    """Picks a lane layout per length class for the bucketed kernel: for each
+    class, times every layout on that class alone (the other classes
+    skipped) and keeps the fastest. The state is laid out in 32-word blocks
+    (the wide kind, 8 lanes). Returns (layouts, table); the engine is left
+    with the plan set, its report set checked against the default kernel's."""
+    layouts = layouts or list(g.LAYOUTS)
+    engine.set_length_plan()
+    engine.set_variant(g.KERNEL_WIDE4, 8, 2, g.VARIANT_PERSISTENT)
+    engine.set_state(state, start, solver_of_word)
+    want = _key(engine.check())
+    table = []
+    best = []
+    for k in range(len(classes)):
+        times = {}
+        for lay in layouts:
+            plan = [g.LAYOUT_SKIP] * len(classes)
+            plan[k] = lay
+            engine.set_length_plan(classes, plan)
+            for _ in range(warmup):
+                engine.launch()
+            engine.wait()
+            engine.kernel_time()
+            engine.set_timing(True)
+            for _ in range(launches):
+                engine.launch()
+            engine.wait()
+            ms, n = engine.kernel_time()
+            engine.set_timing(False)
+            times[lay] = ms / max(n, 1)
+            row = {"class": k, "max_len": int(classes[k]), "layout": lay, "ms": times[lay]}
+            table.append(row)
+            if log:
+                log(json.dumps(row))
+        best.append(min(times, key=times.get))
+    engine.set_length_plan(classes, best)
+    same = _key(engine.check()) == want
+    table.append({"plan": best, "same_reports": same})
+    if not same:
+        raise RuntimeError("the tuned length plan reports differently from the default kernel")
+    return best, table
+
+
 def candidates(n_words):
     c = list(CANDIDATES_DIRECT) + list(CANDIDATES_TILED)
     if n_words >= 8:

@@ -16,6 +16,8 @@ batching: 8e6 clauses (lengths 1 + Zipf(1.2), at most 256), 48 solvers sending
       single      one launch of the default kernel for all batches
       batched     the autotuned persistent kernel for all batches, replayed
                   as a captured CUDA graph
+      bucketed    the bucketed persistent kernel with a lane layout per
+                  length class (tuned class by class), replayed as a graph
     The reports of `batched` and `single` are compared record for record on
     the first pass, and the union of the per-solver launches with `single`'s.
 
@@ -91,6 +93,10 @@ def batching(args):
                                           (g.KERNEL_WIDE4, 8, 4, P), (g.KERNEL_WIDE4, 4, 2, P),
                                           (g.KERNEL_WIDE4, 2, 2, P), (g.KERNEL_WIDE2, 16, 2, P)])
     print(json.dumps({"autotuned": best, "table": table}), flush=True)
+    # bucketed form: a lane layout per length class, tuned class by class
+    plan, ptable = autotune.tune_length_plan(eng, wl.state, start0, wl.solver_of_word)
+    eng.set_length_plan()
+    print(json.dumps({"length_plan": plan, "classes": list(autotune.LENGTH_CLASSES), "table": ptable}), flush=True)
     live = np.arange(wl.n_clauses, dtype=np.int64)
     next_id = wl.n_clauses
     rows = []
@@ -135,13 +141,22 @@ def batching(args):
         eng.set_graph(True)
         got = eng.check() if p == 0 else None
         batched_ms = _timed(eng, eng.launch)
+        # bucketed: the tuned length plan in one persistent launch, as a graph
+        eng.set_variant(g.KERNEL_WIDE4, 8, 2, g.VARIANT_PERSISTENT)
+        eng.set_state(wl.state, start, wl.solver_of_word)
+        eng.set_length_plan(autotune.LENGTH_CLASSES, plan)
+        got_b = eng.check() if p == 0 else None
+        bucketed_ms = _timed(eng, eng.launch)
+        eng.set_length_plan()
         eng.set_graph(False)
         row = {"pass": p, "live_clauses": int(len(live)), "assignments": int(sizes.sum()),
                "checks": checks, "per_solver_ms": per_ms, "single_ms": single_ms, "batched_ms": batched_ms,
                "per_solver_checks_per_s": checks / (per_ms / 1e3), "single_checks_per_s": checks / (single_ms / 1e3),
-               "batched_checks_per_s": checks / (batched_ms / 1e3), "graph_captures": eng.graph_captures}
+               "batched_checks_per_s": checks / (batched_ms / 1e3), "bucketed_ms": bucketed_ms,
+               "bucketed_checks_per_s": checks / (bucketed_ms / 1e3), "graph_captures": eng.graph_captures}
         if p == 0:
             row["batched_equals_single"] = _same(got, ref)
+            row["bucketed_equals_single"] = _same(got_b, ref)
             row["per_solver_union_equals_single"] = _same(np.concatenate(per_solver_reps), ref)
             row["reports"] = int(len(ref))
         rows.append(row)
@@ -151,8 +166,10 @@ def batching(args):
                "per_solver_checks_per_s": float(np.mean([r["per_solver_checks_per_s"] for r in steady])),
                "single_checks_per_s": float(np.mean([r["single_checks_per_s"] for r in steady])),
                "batched_checks_per_s": float(np.mean([r["batched_checks_per_s"] for r in steady])),
-               "exact": bool(rows[0]["batched_equals_single"] and rows[0]["per_solver_union_equals_single"]),
-               "autotuned_variant": best}
+               "bucketed_checks_per_s": float(np.mean([r["bucketed_checks_per_s"] for r in steady])),
+               "exact": bool(rows[0]["batched_equals_single"] and rows[0]["per_solver_union_equals_single"]
+                             and rows[0]["bucketed_equals_single"]),
+               "autotuned_variant": best, "length_plan": plan}
     print(json.dumps(summary), flush=True)
     eng.close()
     return summary

@@ -113,6 +113,22 @@ __device__ __forceinline__ bool clause_live(const CheckArgs &a, uint32_t c) {
     return (__ldg(a.alive + (i >> 5)) >> (i & 31)) & 1u;
 }
 
+// A per-range lane-layout plan for the bucketed kernel (device memory):
+// range k covers scan positions [range_begin[k], range_end[k]) and is checked
+// with lane layout layout[k] (GSS_LAYOUT_*); group_base[k] is the index of
+// its first clause group over all ranges, group_base[n_ranges] their total.
+constexpr uint32_t kMaxRanges = 1024;
+struct BucketPlan {
+    uint32_t n_ranges;
+    uint32_t range_begin[kMaxRanges];
+    uint32_t range_end[kMaxRanges];
+    int32_t layout[kMaxRanges];
+    uint32_t group_base[kMaxRanges + 1];
+};
+int layout_lanes(int layout);  // lanes per clause of a layout, 0 if unknown
+int launch_check_bucketed(const CheckArgs *d_args, const BucketPlan *d_plan, uint32_t *work, cudaStream_t stream,
+                          int sm_count);
+
 // Order-preserving device compaction of a CSR clause database: keeps the
 // clauses whose id (ids[c]) has its bit set in `alive`.
 struct CompactArgs {

@@ -306,6 +306,7 @@ int upload_all(gss_engine *eng) {
 
 // Adds a batch to the host mirror in length order; returns the first index.
 void mirror_append(gss_engine *eng, const int32_t *lits, const int64_t *offsets, int64_t n, const uint32_t *ids) {
+    eng->db_version++;
     std::vector<uint32_t> order;
     length_order(offsets, n, order);
     if (eng->h_off.empty()) eng->h_off.push_back(0);
@@ -447,6 +448,21 @@ int64_t gss_db_live_count(const gss_engine *eng) { return eng ? eng->n_clauses -
 int64_t gss_db_clause_count(const gss_engine *eng) { return eng ? eng->n_clauses : -1; }
 int64_t gss_db_literal_count(const gss_engine *eng) { return eng ? eng->n_lits : -1; }
 int64_t gss_db_max_var(const gss_engine *eng) { return eng ? eng->max_var : -1; }
+
+int gss_engine_set_length_plan(gss_engine *eng, int n_classes, const int32_t *max_len, const int32_t *layout) {
+    if (!eng || n_classes < 0 || (n_classes > 0 && (!max_len || !layout)))
+        return set_error(GSS_ERR_INVALID, "bad arguments to gss_engine_set_length_plan");
+    for (int k = 0; k < n_classes; k++) {
+        if (layout[k] != GSS_LAYOUT_SKIP && layout_lanes(layout[k]) == 0)
+            return set_error(GSS_ERR_INVALID, "unknown lane layout %d", layout[k]);
+        if (k > 0 && max_len[k] <= max_len[k - 1])
+            return set_error(GSS_ERR_INVALID, "class bounds must increase");
+    }
+    eng->plan_max_len.assign(max_len, max_len + n_classes);
+    eng->plan_layout.assign(layout, layout + n_classes);
+    eng->plan_built = ~0ull;
+    return GSS_OK;
+}
 
 int gss_db_positions(const gss_engine *eng, const uint32_t *ids, int64_t n, int64_t *positions) {
     if (!eng || n < 0 || (n > 0 && (!ids || !positions))) return set_error(GSS_ERR_INVALID, "bad arguments");
@@ -624,6 +640,55 @@ int gss_check_launch(gss_engine *eng) {
 
 namespace {
 
+// The position ranges of the length plan over the database as it is now:
+// runs of positions whose clauses fall in one length class (the database is
+// sorted by length, appended batches each sorted), skipped classes left out.
+int build_plan(gss_engine *eng) {
+    if (eng->plan_built == eng->db_version) return GSS_OK;
+    static_assert(sizeof(BucketPlan) < (1u << 20), "plan size");
+    std::vector<BucketPlan> hp(1);
+    BucketPlan &p = hp[0];
+    memset(&p, 0, sizeof p);
+    const std::vector<int32_t> &bound = eng->plan_max_len;
+    const int n_classes = (int) bound.size();
+    int prev_class = -1;
+    uint32_t groups = 0;
+    auto close_range = [&]() {
+        if (p.n_ranges == 0) return;
+        const uint32_t k = p.n_ranges - 1;
+        const uint32_t cpw = 32u / (uint32_t) layout_lanes(p.layout[k]);
+        p.group_base[k] = groups;
+        groups += (p.range_end[k] - p.range_begin[k] + cpw - 1) / cpw;
+    };
+    for (int64_t c = 0; c < eng->n_clauses; c++) {
+        const int32_t len = (int32_t) (eng->h_off[c + 1] - eng->h_off[c]);
+        int cls = (int) (std::lower_bound(bound.begin(), bound.end(), len) - bound.begin());
+        if (cls >= n_classes) cls = n_classes - 1;
+        if (cls == prev_class && p.n_ranges > 0 && p.range_end[p.n_ranges - 1] == (uint32_t) c) {
+            p.range_end[p.n_ranges - 1] = (uint32_t) (c + 1);
+            continue;
+        }
+        prev_class = cls;
+        if (eng->plan_layout[cls] == GSS_LAYOUT_SKIP) continue;
+        if (p.n_ranges == kMaxRanges)
+            return set_error(GSS_ERR_STATE, "the length plan needs more than %u position ranges (compact the database)",
+                             kMaxRanges);
+        close_range();
+        p.range_begin[p.n_ranges] = (uint32_t) c;
+        p.range_end[p.n_ranges] = (uint32_t) (c + 1);
+        p.layout[p.n_ranges] = eng->plan_layout[cls];
+        p.n_ranges++;
+    }
+    close_range();
+    p.group_base[p.n_ranges] = groups;
+    GSS_TRY(eng->d_plan.reserve(sizeof(BucketPlan)));
+    GSS_CUDA_TRY(cudaMemcpyAsync(eng->d_plan.ptr, &p, sizeof(BucketPlan), cudaMemcpyHostToDevice, eng->stream));
+    GSS_CUDA_TRY(cudaStreamSynchronize(eng->stream));  // pageable source
+    eng->plan_ranges = p.n_ranges;
+    eng->plan_built = eng->db_version;
+    return GSS_OK;
+}
+
 int launch_pass_into(gss_engine *eng, const void *state, DevBuf &reports, DevBuf &counts, PinnedBuf &h_counts) {
     order_quiesce(eng);  // a scoring in flight reads the buffers this pass may reallocate
     if (eng->n_clauses > 0 && eng->max_var >= eng->n_vars)
@@ -689,13 +754,18 @@ int launch_pass_into(gss_engine *eng, const void *state, DevBuf &reports, DevBuf
     }
     const bool wide = eng->state_kind == GSS_KERNEL_WIDE4 || eng->state_kind == GSS_KERNEL_WIDE2;
     const bool ordered = order_active(eng);
-    if (ordered && (eng->state_kind == GSS_KERNEL_TILED || (eng->flags & GSS_VARIANT_PERSISTENT)))
-        return set_error(GSS_ERR_STATE, "the learned scan order runs the direct and wide kernels (not the tiled or "
-                         "persistent ones)");
+    const bool bucketed = !eng->plan_layout.empty();
+    if (ordered && (eng->state_kind == GSS_KERNEL_TILED || (eng->flags & GSS_VARIANT_PERSISTENT) || bucketed))
+        return set_error(GSS_ERR_STATE, "the learned scan order runs the direct and wide kernels (not the tiled, "
+                         "persistent or bucketed ones)");
+    if (bucketed && eng->n_words > 0 && eng->state_bw != 32)
+        return set_error(GSS_ERR_STATE, "the length plan needs a state laid out in 32-word blocks (%d here)",
+                         eng->state_bw);
     if (ordered && (&reports != &eng->reports || &counts != &eng->counts))
         return set_error(GSS_ERR_STATE, "the learned scan order runs through gss_check_launch");
-    if (wide && (eng->flags & GSS_VARIANT_PERSISTENT)) {
+    if (bucketed || (wide && (eng->flags & GSS_VARIANT_PERSISTENT))) {
         // arguments through device memory, so the same graph serves every pass
+        if (bucketed) GSS_TRY(build_plan(eng));
         GSS_TRY(eng->d_args.reserve(sizeof(CheckArgs)));
         GSS_TRY(eng->work.reserve(sizeof(uint32_t)));
         GSS_CUDA_TRY(cudaMemcpyAsync(eng->d_args.ptr, &a, sizeof a, cudaMemcpyHostToDevice, eng->stream));
@@ -704,10 +774,18 @@ int launch_pass_into(gss_engine *eng, const void *state, DevBuf &reports, DevBuf
             GSS_CUDA_TRY(cudaMemsetAsync(a.counts, 0, sizeof(uint32_t) * a.n_parts, eng->stream));
             GSS_CUDA_TRY(cudaMemsetAsync(a.err, 0, sizeof(uint32_t), eng->stream));
             GSS_CUDA_TRY(cudaMemsetAsync(eng->work.ptr, 0, sizeof(uint32_t), eng->stream));
-            if (a.n_clauses > 0 && a.n_blocks > 0)
-                GSS_TRY(launch_check_wide_persist((const CheckArgs *) eng->d_args.ptr, words_per_lane(eng->state_kind),
-                                                  eng->state_lpc, eng->state_g, (uint32_t *) eng->work.ptr,
-                                                  eng->stream, eng->sm_count));
+            if (a.n_clauses > 0 && a.n_blocks > 0) {
+                if (bucketed) {
+                    if (eng->plan_ranges > 0)
+                        GSS_TRY(launch_check_bucketed((const CheckArgs *) eng->d_args.ptr,
+                                                      (const BucketPlan *) eng->d_plan.ptr, (uint32_t *) eng->work.ptr,
+                                                      eng->stream, eng->sm_count));
+                } else {
+                    GSS_TRY(launch_check_wide_persist((const CheckArgs *) eng->d_args.ptr,
+                                                      words_per_lane(eng->state_kind), eng->state_lpc, eng->state_g,
+                                                      (uint32_t *) eng->work.ptr, eng->stream, eng->sm_count));
+                }
+            }
             GSS_CUDA_TRY(cudaMemcpyAsync(h_counts.ptr, counts.ptr, sizeof(uint32_t) * eng->n_parts,
                                          cudaMemcpyDeviceToHost, eng->stream));
             GSS_CUDA_TRY(cudaMemcpyAsync((uint32_t *) h_counts.ptr + eng->n_parts, a.err, sizeof(uint32_t),
@@ -718,7 +796,8 @@ int launch_pass_into(gss_engine *eng, const void *state, DevBuf &reports, DevBuf
             const std::vector<uintptr_t> key = {
                 (uintptr_t) a.counts, (uintptr_t) h_counts.ptr, (uintptr_t) a.err, (uintptr_t) eng->work.ptr,
                 (uintptr_t) eng->d_args.ptr, (uintptr_t) eng->state_kind, (uintptr_t) eng->state_lpc,
-                (uintptr_t) eng->state_g, (uintptr_t) eng->n_parts, (uintptr_t) (a.n_clauses > 0 && a.n_blocks > 0)};
+                (uintptr_t) eng->state_g, (uintptr_t) eng->n_parts, (uintptr_t) (a.n_clauses > 0 && a.n_blocks > 0),
+                (uintptr_t) bucketed, (uintptr_t) eng->d_plan.ptr, (uintptr_t) (eng->plan_ranges > 0)};
             if (key != eng->graph_key || !eng->graph_exec) {
                 if (eng->graph_exec) cudaGraphExecDestroy(eng->graph_exec);
                 if (eng->graph) cudaGraphDestroy(eng->graph);

@@ -78,6 +78,14 @@ struct gss_engine {
     // CUDA graph of a pass (memsets, kernel, count readback), recaptured when
     // a buffer it names changes
     DevBuf d_args, work;
+    // length plan of the bucketed kernel (gss_engine_set_length_plan): class
+    // bounds and lane layouts; the position ranges are rebuilt on the device
+    // when plan_built differs from db_version
+    std::vector<int32_t> plan_max_len, plan_layout;
+    DevBuf d_plan;
+    uint64_t db_version = 0;  // counts every change of the database's positions
+    uint64_t plan_built = ~0ull;
+    uint32_t plan_ranges = 0;
     bool use_graph = false;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;

@@ -104,6 +104,25 @@ int gss_engine_kernel_time(gss_engine *eng, double *total_ms, int64_t *n_launche
 #define GSS_VARIANT_PIPELINED 4  /* wide kinds: next clause's offsets and literals loaded ahead */
 #define GSS_VARIANT_PERSISTENT 8 /* wide kinds: one CTA set for the whole pass, tasks from a work counter,
                                     arguments from device memory (what gss_engine_set_graph replays) */
+/* Lane layouts of the bucketed kernel (gss_engine_set_length_plan): words
+ * per lane x lanes per clause (always one 32-word state row per slot block),
+ * and loads in flight per lane. GSS_LAYOUT_SKIP leaves a length class out of
+ * the pass (for timing the others). */
+#define GSS_LAYOUT_SKIP -1
+#define GSS_LAYOUT_4x8_G1 0
+#define GSS_LAYOUT_4x8_G2 1
+#define GSS_LAYOUT_2x16_G1 2
+#define GSS_LAYOUT_2x16_G2 3
+#define GSS_LAYOUT_1x32_G1 4
+#define GSS_LAYOUT_1x32_G2 5
+/* Length plan: the pass checks clauses of length in (max_len[k-1],
+ * max_len[k]] (class k; the last class takes everything longer too) with
+ * lane layout layout[k], all classes in one persistent launch (the bucketed
+ * kernel, arguments and plan in device memory, replayed as a CUDA graph when
+ * gss_engine_set_graph is on). Needs a state laid out in 32-word blocks (the
+ * wide kinds with 8 or 16 lanes, or the direct kind with 32). n_classes = 0
+ * turns the plan off. gpusharesat_gb300.autotune picks the layouts. */
+int gss_engine_set_length_plan(gss_engine *eng, int n_classes, const int32_t *max_len, const int32_t *layout);
 /* Selects the check-kernel variant. A group of lanes_per_clause lanes checks
  * one clause against a slot block of lanes_per_clause x (words per lane)
  * 32-slot words (0 = automatic: one word per lane up to a full warp, or 32

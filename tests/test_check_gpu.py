@@ -300,3 +300,78 @@ def test_persistent_graph_replays_across_passes(engine):
         engine.set_graph(False)
         engine.set_capacity(0)
         engine.set_variant()
+
+
+# ---- the bucketed kernel: a lane layout per length class ----
+
+def _plan_engine(wl):
+    import gpusharesat_gb300 as g
+    eng = g.Engine(0)
+    eng.set_db(wl.lits, wl.offsets)
+    eng.set_variant(g.KERNEL_WIDE4, 8, 2, g.VARIANT_PERSISTENT)
+    eng.set_state(wl.state, wl.start, wl.solver_of_word)
+    return eng
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_length_plan_matches_oracle(lib, seed):
+    """Random layouts per length class, 32 and 96 words: the bucketed pass
+    reports exactly what the oracle reports."""
+    import gpusharesat_gb300 as g
+    rng = np.random.default_rng(seed)
+    n_solvers = 16 if seed < 2 else 48
+    wl = W.make_scale(seed=40 + seed, n_vars=2 ** 13, n_clauses=30000, n_solvers=n_solvers)
+    if seed == 2:  # two words per solver, as the batching workload
+        wl = W.make_batching(seed=42, n_vars=2 ** 13, n_clauses=30000, n_solvers=48)
+    eng = _plan_engine(wl)
+    ref = oracle.check(wl.lits, wl.offsets, wl.state, wl.start)
+    for _ in range(3):
+        layouts = rng.choice(g.LAYOUTS, size=4).tolist()
+        eng.set_length_plan((4, 12, 32, 1 << 30), layouts)
+        _assert_same(g.sort_reports(eng.check()), ref, wl)
+    eng.set_length_plan()
+    _assert_same(g.sort_reports(eng.check()), ref, wl)
+    eng.close()
+
+
+def test_length_plan_skips_classes(lib):
+    import gpusharesat_gb300 as g
+    wl = W.make_scale(seed=44, n_vars=2 ** 13, n_clauses=30000, n_solvers=32)
+    eng = _plan_engine(wl)
+    ref = oracle.check(wl.lits, wl.offsets, wl.state, wl.start)
+    lens = np.diff(wl.offsets)
+    eng.set_length_plan((4, 12, 32, 1 << 30), [g.LAYOUT_SKIP, g.LAYOUT_4x8_G2, g.LAYOUT_SKIP, g.LAYOUT_1x32_G1])
+    keep = ((lens > 4) & (lens <= 12)) | (lens > 32)
+    _assert_same(g.sort_reports(eng.check()), ref[keep[ref["clause"]]], wl)
+    eng.close()
+
+
+def test_length_plan_with_churn_and_graph(lib):
+    """Appended batches (each sorted) make many position ranges; deletes are
+    skipped in the kernel; the plan is rebuilt after each change and the
+    pass graph replays it."""
+    import gpusharesat_gb300 as g
+    rng = np.random.default_rng(45)
+    base = W.make_scale(seed=45, n_vars=2 ** 12, n_clauses=20000, n_solvers=32)
+    live = {c: base.lits[base.offsets[c]:base.offsets[c + 1]].tolist() for c in range(base.n_clauses)}
+    eng = _plan_engine(base)
+    eng.set_graph(True)
+    eng.set_length_plan((3, 8, 20, 1 << 30), [g.LAYOUT_1x32_G2, g.LAYOUT_2x16_G1, g.LAYOUT_4x8_G2, g.LAYOUT_4x8_G1])
+    next_id = base.n_clauses
+    for step in range(4):
+        gone = rng.choice(sorted(live), size=800, replace=False)
+        eng.delete(gone)
+        for i in gone:
+            del live[int(i)]
+        lits, offs = W.distinct_var_clauses(rng, W.lengths_small(rng, 900), base.n_vars)
+        eng.append_db(lits, offs)
+        for k in range(900):
+            live[next_id + k] = lits[offs[k]:offs[k + 1]].tolist()
+        next_id += 900
+        got = np.sort(eng.check(), order=["clause", "word"])
+        ref = _live_reference(live, base.state, base.start)
+        assert len(got) == len(ref)
+        for f in ("clause", "word", "mask"):
+            np.testing.assert_array_equal(got[f], ref[f])
+    assert eng.graph_captures >= 1
+    eng.close()
