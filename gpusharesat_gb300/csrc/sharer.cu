@@ -605,9 +605,10 @@ int Sharer::compact_device() {
 
 void Sharer::evict(int64_t n) {
     // Oldest first among the clauses not reported in the last kRecentPasses
-    // passes; then, if that is not enough, the oldest of the rest. Age is the
-    // device order: arrival order, except that a reduceDb sorts its survivors
-    // by length. evict_cursor_ is the oldest live clause that round 0 may
+    // passes (the first sweep); then, if that is not enough, the oldest of
+    // the rest (the second). Age is the order of meta_ (the device order
+    // keeps it): arrival order, except that a reduceDb sorts its survivors by
+    // length. evict_cursor_ is the oldest live clause the first sweep may
     // still take (the oldest one it skipped as recently reported, or the one
     // after the last it took).
     constexpr int32_t kRecentPasses = 8;
