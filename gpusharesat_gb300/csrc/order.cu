@@ -4,12 +4,13 @@
 // checked each pass: the report set is the plain scan's.
 //
 // Per pass (score_pass):
-//   1-2. score_kernel, one warp per 16 clause positions: folds each clause's
-//      report count of the previous pass into its 8-pass history (a byte per
+//   1-2. score_kernel, a lane per clause position (a warp per 32): folds the
+//      clause's report count of pass q-2 into its 8-pass history (a byte per
 //      pass; the first time an id is seen, its birth), logs a sample of
-//      (features, reported) rows for training, computes the features, runs
-//      the MLP on tensor cores (mma.sync m16n8k16, BF16 operands, FP32
-//      accumulation) and writes the clause's score bucket
+//      (features, reported) rows for training, computes the features; the
+//      warp runs the MLP on tensor cores (mma.sync m16n8k16, BF16 operands,
+//      FP32 accumulation) over its 32 clauses as two m16 tiles, and each lane
+//      writes its clause's score bucket
 //   3. bucket_hist_kernel, bucket_scan_kernel, head_key_kernel, then a
 //      stable one-digit radix sort of positions (bucket_hist, bucket_scan,
 //      bucket_base, bucket_scatter) by key: the score bucket for the clauses
@@ -25,9 +26,11 @@
 // (each clause keeps two counters, for even and odd passes). Calls that
 // change the engine's buffers wait for it first (order_quiesce).
 //
-// Training (every retrain_interval passes, and gss_scorer_train_step): FP32
-// forward and backward kernels over a minibatch, a gradient kernel (one
-// thread per parameter, no atomics), and Adam.
+// Training (every retrain_interval passes, on a stream of its own, over a
+// snapshot of the log; and gss_scorer_train_step): FP32 forward and backward
+// kernels over a minibatch, per-32-row partial gradients reduced in a fixed
+// order (no atomics), and Adam. The passes take the new weights once the
+// training is done.
 #include <cuda_bf16.h>
 #include <math.h>
 #include <string.h>
