@@ -7,7 +7,9 @@ library (``gpusharesat_gb300``) never imports it and has no CPU fallback.
 ``check()`` wraps ``oracle/check.c``, a C restatement of the report rule of
 gpuShareLib/GpuRunner.cu:34-89 (see that file's header for the mapping).
 ``sharer_model`` restates the host-side state machine of the
-``GpuClauseSharer`` API in plain Python for small cases.
+``GpuClauseSharer`` API in plain Python for small cases. ``mlp`` restates
+the learned scan order's scorer (forward, loss, gradient, Adam, BF16
+inference) and its per-clause features in float64 numpy.
 """
 import ctypes
 import os
