@@ -59,6 +59,9 @@ def parse():
     p.add_argument("--lpc", type=int, default=0, help="lanes per clause (0 = automatic)")
     p.add_argument("--depth", type=int, default=4, help="loads in flight (direct) or clause slots (tiled)")
     p.add_argument("--flags", type=int, default=0, help="variant flags (1: L2 hint, 2: occupancy)")
+    p.add_argument("--locality", type=int, default=-1,
+                   help="database order: -1 automatic variable ranges, 0 length order, 11..31 ranges of 2^n vars")
+    p.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     return p.parse_args()
 
 
@@ -194,10 +197,29 @@ def job_throughput(units_per_rank_per_step, world, max_seconds_per_step):
     return units_per_rank_per_step * world / max_seconds_per_step
 
 
+def cpu_parity(wl, gpu_reports, threads=None):
+    """CPU leg, part 1: the oracle (C restatement, all host cores) checks the
+    whole workload once, outside the timed region, and its records are
+    compared field by field with the GPU's sizing pass (clause, word, mask,
+    and the solver of the word)."""
+    import oracle
+    import gpusharesat_gb300 as g
+    threads = threads or os.cpu_count() or 1
+    ref = oracle.check(wl.lits, wl.offsets, wl.state, wl.start, n_threads=threads)
+    got = g.sort_reports(gpu_reports)
+    mism = abs(len(got) - len(ref))
+    if len(got) == len(ref):
+        bad = (got["clause"] != ref["clause"]) | (got["word"] != ref["word"]) | (got["mask"] != ref["mask"]) | \
+            (got["solver"] != wl.solver_of_word[ref["word"]].astype(np.uint32))
+        mism = int(bad.sum())
+    return {"records": int(len(ref)), "gpu_records": int(len(got)), "mismatches": int(mism),
+            "checker": "oracle/check.c (C restatement of gpuShareLib/GpuRunner.cu:34-89), full workload"}
+
+
 def cpu_baseline(wl, seconds, threads=None):
-    """Times the oracle (C restatement, all host cores) on a prefix of the
-    clause database sized to take about `seconds`. Returns checks/s and the
-    sample description."""
+    """CPU leg, part 2: times the oracle (C restatement, all host cores) on a
+    prefix of the clause database sized to take about `seconds`. Returns
+    checks/s and the sample description."""
     import oracle
     threads = threads or os.cpu_count() or 1
     n = min(wl.n_clauses, 20000)
@@ -277,12 +299,13 @@ def run_gpu(args):
     eng.set_stream(stream.cuda_stream)
     if args.kind is not None:
         eng.set_variant(args.kind, args.lpc, args.depth, args.flags)
+    eng.set_locality(args.locality)
     eng.set_db(wl.lits, wl.offsets)
     eng.set_state(wl.state, wl.start, wl.solver_of_word)
-    # size the queues: run once (grows on overflow)
-    rep = eng.check()
-    n_reports = len(rep)
-    del rep
+    # size the queues: run once (grows on overflow); its reports are checked
+    # against the oracle in the CPU leg, after the timed regions
+    sizing_reports = eng.check()
+    n_reports = len(sizing_reports)
 
     # ---- device-resident timing (value) ----
     for _ in range(args.warmup):
@@ -337,13 +360,15 @@ def run_gpu(args):
         g._check(rc)
         assert all(nrep[i] == n_reports for i in range(k)), list(nrep)
 
-    e2e_run(max(2, args.warmup))
-    barrier()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    e2e_run(args.e2e_steps)
-    torch.cuda.synchronize()
-    e2e_s = max_over_ranks((time.perf_counter() - t0) / args.e2e_steps, world, "cuda")
+    e2e_s = float("nan")
+    if not args.no_e2e:
+        e2e_run(max(2, args.warmup))
+        barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_run(args.e2e_steps)
+        torch.cuda.synchronize()
+        e2e_s = max_over_ranks((time.perf_counter() - t0) / args.e2e_steps, world, "cuda")
     h2d = wl.state.nbytes + wl.start.nbytes + wl.solver_of_word.nbytes
     d2h = n_reports * 16 + 16 * 4
 
@@ -352,10 +377,14 @@ def run_gpu(args):
         kern_avg_s = (kern_ms / max(kern_n, 1)) / 1e3
         B = algorithmic_bytes(wl, n_reports)
         achieved = B / kern_avg_s / 1e9
+        traffic = load_traffic() if (args.workload == "scale" and args.clauses == 4_000_000
+                                     and args.kind is None and args.locality == -1) else None
         roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                     "frac": achieved / peak,
-                    "traffic": load_traffic() if (args.workload == "scale" and args.clauses == 4_000_000
-                                                  and args.kind is None) else None,
+                    "traffic": traffic,
+                    "traffic_source": ("ncu capture of this kernel on this workload, committed summary "
+                                       "profiles/check_wide_kernel_plain_scale.md (not measured in this run)")
+                    if traffic else None,
                     "algorithmic_bytes_per_launch": B, "kernel_ms": kern_avg_s * 1e3,
                     "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                     else "fallback"}
@@ -366,12 +395,14 @@ def run_gpu(args):
             "config": config_dict(args, world),
             "reports_per_pass": n_reports,
             "e2e": {"value": job_throughput(checks_per_pass, world, e2e_s), "unit": UNIT, "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3},
+                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3} if not args.no_e2e else None,
+            "database_order": {"locality_shift": eng.locality_shift},
             "roofline": roofline,
             "gpu_launches": gpu_launches,
             "clocks": clocks,
         }
         if not args.no_cpu_baseline:
+            line["parity"] = cpu_parity(wl, sizing_reports)
             v, cores, sample = cpu_baseline(wl, args.cpu_seconds)
             line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
         print(json.dumps(line), flush=True)

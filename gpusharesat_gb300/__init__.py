@@ -73,6 +73,7 @@ def load():
     c_int, c_i64, vp = ctypes.c_int, ctypes.c_int64, ctypes.c_void_p
     _sig(lib, "gss_last_error", ctypes.c_char_p)
     _sig(lib, "gss_version", ctypes.c_char_p)
+    _sig(lib, "gss_debug_fail_device_alloc", c_int, c_i64, c_int)
     _sig(lib, "gss_max_clause_len", c_int)
     _sig(lib, "gss_engine_create", c_int, c_int, vp)
     _sig(lib, "gss_engine_destroy", c_int, vp)
@@ -88,6 +89,8 @@ def load():
     _sig(lib, "gss_db_append", c_int, vp, vp, vp, c_i64, vp)
     _sig(lib, "gss_db_delete", c_int, vp, vp, c_i64)
     _sig(lib, "gss_db_compact", c_int, vp)
+    _sig(lib, "gss_db_set_locality", c_int, vp, c_int)
+    _sig(lib, "gss_db_locality_shift", c_int, vp)
     _sig(lib, "gss_db_live_count", c_i64, vp)
     _sig(lib, "gss_db_literal_count", c_i64, vp)
     _sig(lib, "gss_db_max_var", c_i64, vp)
@@ -124,6 +127,13 @@ def load():
     _sig(lib, "gss_bench_plant", c_int, vp, vp, c_i64, vp, vp, vp, c_i64, c_int, ctypes.c_uint64, c_i64, c_int, vp)
     _lib = lib
     return lib
+
+
+def debug_fail_device_alloc(min_bytes, count=1):
+    """Testing hook: the next `count` device allocations of at least
+    `min_bytes` fail as if the GPU were out of memory (made on the host;
+    count=0 turns it off)."""
+    _check(load().gss_debug_fail_device_alloc(int(min_bytes), int(count)))
 
 
 def _check(rc):
@@ -206,6 +216,17 @@ class Engine:
 
     def compact(self):
         _check(self.lib.gss_db_compact(self.h))
+
+    def set_locality(self, range_log2=-1):
+        """Database order from the next set_db/append_db/compact: -1 automatic
+        variable ranges, 0 length order only, 11..31 ranges of 2^range_log2
+        variables (see gss_db_set_locality)."""
+        _check(self.lib.gss_db_set_locality(self.h, int(range_log2)))
+
+    @property
+    def locality_shift(self):
+        """log2 of the variables per range of the current order (0: length order)."""
+        return int(self.lib.gss_db_locality_shift(self.h))
 
     @property
     def live_count(self):

@@ -36,7 +36,6 @@
 // partition keeps counting, so the host sees the overflow and runs again.
 #include <string.h>
 
-#include <mutex>
 
 #include "common.h"
 
@@ -848,30 +847,18 @@ int launch_relayout(const uint2 *src, uint2 *dst, uint32_t n_vars, uint32_t n_wo
 namespace {
 
 constexpr uint32_t kNoAllocMaxParts = 64;
-constexpr int kNoAllocMaxDevices = 64;
 
 // Report reservation counters of gss_check_noalloc, shared by all its calls.
 static __device__ __align__(256) uint32_t g_noalloc_counters[kNoAllocMaxParts];
 
-std::mutex g_noalloc_lock;
-void *g_noalloc_addr[kNoAllocMaxDevices];  // device address of the counters, per device
-
 // The counters' device address on the current device. In host code the
-// array's name is only a host-side stand-in; the first call on a device asks
-// the runtime for the real address and keeps it.
+// array's name is only a host-side stand-in, so every call asks the runtime
+// for the real address (a host-side lookup: it allocates nothing, and it
+// stays right if the device's context is torn down and created again).
 int noalloc_counters(uint32_t **out) {
-    int dev = 0;
-    GSS_CUDA_TRY(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= kNoAllocMaxDevices)
-        return gss::set_error(GSS_ERR_INVALID, "device %d: the allocation-free pass supports devices 0..%d", dev,
-                              kNoAllocMaxDevices - 1);
-    std::lock_guard<std::mutex> g(g_noalloc_lock);
-    if (!g_noalloc_addr[dev]) {
-        void *p = nullptr;
-        GSS_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_counters));
-        g_noalloc_addr[dev] = p;
-    }
-    *out = (uint32_t *) g_noalloc_addr[dev];
+    void *p = nullptr;
+    GSS_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_counters));
+    *out = (uint32_t *) p;
     return GSS_OK;
 }
 
@@ -891,6 +878,8 @@ extern "C" int gss_check_noalloc(const int32_t *lits, const int64_t *offsets, ui
                                                                                   !solver_of_word)) ||
         (cap_per_part > 0 && !out))
         return set_error(GSS_ERR_INVALID, "gss_check_noalloc: NULL input or output");
+    if (n_clauses > 0 && n_vars == 0)
+        return set_error(GSS_ERR_INVALID, "gss_check_noalloc: %u clauses over 0 variables", n_clauses);
     if ((uint64_t) cap_per_part * n_parts > 0xFFFFFFFFull)
         return set_error(GSS_ERR_INVALID, "gss_check_noalloc: output capacity above 2^32 records");
     cudaStream_t st = (cudaStream_t) stream;

@@ -117,7 +117,7 @@ __device__ __forceinline__ bool clause_live(const CheckArgs &a, uint32_t c) {
 // range k covers scan positions [range_begin[k], range_end[k]) and is checked
 // with lane layout layout[k] (GSS_LAYOUT_*); group_base[k] is the index of
 // its first clause group over all ranges, group_base[n_ranges] their total.
-constexpr uint32_t kMaxRanges = 1024;
+constexpr uint32_t kMaxRanges = 8192;
 struct BucketPlan {
     uint32_t n_ranges;
     uint32_t range_begin[kMaxRanges];

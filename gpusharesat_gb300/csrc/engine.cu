@@ -5,6 +5,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <mutex>
 #include <vector>
 
@@ -25,11 +26,24 @@ int set_error(int code, const char *fmt, ...) {
     return code;
 }
 
+// Host-side fault injection for tests (gss_debug_fail_device_alloc): the
+// next `count` device allocations of at least `min_bytes` made through DevBuf
+// fail as if the device were out of memory. Nothing reaches the GPU.
+static std::atomic<int64_t> g_fail_min_bytes{0};
+static std::atomic<int> g_fail_count{0};
+
+bool injected_alloc_failure(size_t bytes) {
+    if (g_fail_count.load() <= 0 || (int64_t) bytes < g_fail_min_bytes.load()) return false;
+    return g_fail_count.fetch_sub(1) > 0;
+}
+
 int DevBuf::reserve(size_t need) {
     if (need <= bytes && ptr) return GSS_OK;
     release();
     size_t cap = 256;
     while (cap < need) cap *= 2;
+    if (injected_alloc_failure(cap))
+        return set_error(GSS_ERR_NOMEM, "cudaMalloc(%zu) failed: out of memory (injected)", cap);
     cudaError_t e = cudaMalloc(&ptr, cap);
     if (e != cudaSuccess) {
         ptr = nullptr;
@@ -44,6 +58,8 @@ int DevBuf::grow_keep(size_t need, cudaStream_t stream, size_t keep_bytes) {
     if (need <= bytes && ptr) return GSS_OK;
     size_t cap = bytes ? bytes : 256;
     while (cap < need) cap *= 2;
+    if (injected_alloc_failure(cap))
+        return set_error(GSS_ERR_NOMEM, "cudaMalloc(%zu) failed: out of memory (injected)", cap);
     void *np = nullptr;
     cudaError_t e = cudaMalloc(&np, cap);
     if (e != cudaSuccess) {
@@ -125,6 +141,13 @@ extern "C" {
 const char *gss_last_error(void) { return g_last_error.c_str(); }
 
 const char *gss_version(void) { return "gpusharesat-gb300 0.1 sm_103a"; }
+
+int gss_debug_fail_device_alloc(int64_t min_bytes, int count) {
+    if (count < 0 || min_bytes < 0) return set_error(GSS_ERR_INVALID, "bad arguments to gss_debug_fail_device_alloc");
+    g_fail_min_bytes = min_bytes;
+    g_fail_count = count;
+    return GSS_OK;
+}
 
 int gss_max_clause_len(void) { return kMaxClauseLen; }
 
@@ -304,16 +327,86 @@ int upload_all(gss_engine *eng) {
     return GSS_OK;
 }
 
-// Adds a batch to the host mirror in length order; returns the first index.
-void mirror_append(gss_engine *eng, const int32_t *lits, const int64_t *offsets, int64_t n, const uint32_t *ids) {
+// Variable-range order of a batch. The variables are cut into ranges of
+// 2^shift; each clause's literals are reordered by how many of them fall in
+// their range (the most frequent range first, ties by range; stable inside a
+// range), and the clauses are ordered by (first range, second range, length,
+// batch order). Warps that run side by side then gather the state rows of
+// one or two ranges for their first literals, a working set that stays in
+// L2, where a length-only order gathers rows from the whole state. The rule
+// is a symmetric function of a clause's literal values, so neither order
+// changes a report. `relits` receives the batch's literals, each clause's
+// reordered in place (same offsets as the batch).
+void range_order(const int32_t *lits, const int64_t *offsets, int64_t n, int shift, std::vector<uint32_t> &order,
+                 std::vector<int32_t> &relits) {
+    std::vector<std::pair<uint64_t, uint32_t>> keys((size_t) n);
+    std::vector<std::pair<int32_t, int32_t>> cnt;  // (range, count) of one clause
+    const int64_t base = n > 0 ? offsets[0] : 0;
+    relits.resize((size_t) (n > 0 ? offsets[n] - base : 0));
+    for (int64_t c = 0; c < n; c++) {
+        const int64_t b = offsets[c], e = offsets[c + 1];
+        cnt.clear();
+        for (int64_t i = b; i < e; i++) {
+            const int32_t r = (int32_t) ((uint32_t) lits[i] >> 1 >> shift);
+            bool found = false;
+            for (auto &p : cnt)
+                if (p.first == r) {
+                    p.second++;
+                    found = true;
+                    break;
+                }
+            if (!found) cnt.push_back({r, 1});
+        }
+        std::sort(cnt.begin(), cnt.end(), [](const std::pair<int32_t, int32_t> &x, const std::pair<int32_t, int32_t> &y) {
+            return x.second != y.second ? x.second > y.second : x.first < y.first;
+        });
+        int64_t o = b - base;
+        for (const auto &p : cnt)
+            for (int64_t i = b; i < e; i++)
+                if ((int32_t) ((uint32_t) lits[i] >> 1 >> shift) == p.first) relits[(size_t) o++] = lits[i];
+        const uint64_t home = (uint64_t) cnt[0].first;
+        const uint64_t second = cnt.size() > 1 ? (uint64_t) cnt[1].first : home;
+        // 20 bits per range index (ranges of 2^11 variables or more), 13 for the length
+        keys[c] = {(home << 33) | (second << 13) | (uint64_t) (e - b), (uint32_t) c};
+    }
+    std::sort(keys.begin(), keys.end());
+    order.resize((size_t) n);
+    for (int64_t k = 0; k < n; k++) order[k] = keys[k].second;
+}
+
+// log2 of the variables per range for a database whose largest variable is
+// max_var: ranges of 2^17 variables (32 MB of state rows at 32 words per
+// block) by default; 0 (no ranges) when there would be a single range.
+int effective_range_shift(const gss_engine *eng, int64_t max_var) {
+    int shift = eng->range_log2 < 0 ? 17 : eng->range_log2;
+    if (shift == 0 || max_var < 0 || (max_var >> shift) == 0) return 0;
+    return shift;
+}
+
+// Adds a batch to the host mirror in length order (or variable-range order,
+// see range_order); returns the first index.
+void mirror_append(gss_engine *eng, const int32_t *lits, const int64_t *offsets, int64_t n, const uint32_t *ids,
+                   int64_t max_var) {
     eng->db_version++;
     std::vector<uint32_t> order;
-    length_order(offsets, n, order);
+    std::vector<int32_t> relits;
+    const int shift = effective_range_shift(eng, max_var);
+    const int32_t *src = lits;
+    int64_t src_base = 0;  // offsets[c] - src_base indexes src
+    if (shift > 0) {
+        range_order(lits, offsets, n, shift, order, relits);
+        src = relits.data();
+        src_base = n > 0 ? offsets[0] : 0;
+    } else {
+        length_order(offsets, n, order);
+    }
     if (eng->h_off.empty()) eng->h_off.push_back(0);
+    eng->h_lits.reserve(eng->h_lits.size() + (size_t) (n > 0 ? offsets[n] - offsets[0] : 0));
     for (int64_t k = 0; k < n; k++) {
         const int64_t c = order[k];
         const int64_t len = offsets[c + 1] - offsets[c];
-        eng->h_lits.insert(eng->h_lits.end(), lits + offsets[c], lits + offsets[c] + len);
+        const int32_t *cl = src + (offsets[c] - src_base);
+        eng->h_lits.insert(eng->h_lits.end(), cl, cl + len);
         eng->h_off.push_back(eng->h_off.back() + len);
         const uint32_t id = ids ? ids[c] : (uint32_t) (eng->next_id + c);
         if (id >= eng->index_of.size()) eng->index_of.resize((size_t) id + 1 + (id >> 3), 0xFFFFFFFFu);
@@ -345,7 +438,7 @@ int gss_db_set(gss_engine *eng, const int32_t *lits, const int64_t *offsets, int
     eng->next_id = 0;
     eng->db_epoch++;
     eng->layout_epoch++;
-    mirror_append(eng, lits, offsets, n_clauses, nullptr);
+    mirror_append(eng, lits, offsets, n_clauses, nullptr, max_var);
     GSS_TRY(upload_all(eng));
     eng->max_var = max_var;
     return GSS_OK;
@@ -367,7 +460,7 @@ int gss_db_append(gss_engine *eng, const int32_t *lits, const int64_t *offsets, 
     }
     const int64_t base = eng->h_off.empty() ? 0 : eng->h_off.back();
     if (base + offsets[n_clauses] > 0x7FFFFF00LL) return set_error(GSS_ERR_INVALID, "too many literals");
-    mirror_append(eng, lits, offsets, n_clauses, ids);
+    mirror_append(eng, lits, offsets, n_clauses, ids, std::max(eng->max_var, max_var));
     const int64_t n = (int64_t) eng->h_ids.size();
     const int64_t n_lits = eng->h_off.back();
     GSS_TRY(ensure_device(eng));
@@ -438,10 +531,20 @@ int gss_db_compact(gss_engine *eng) {
     eng->h_off.assign(1, 0);
     eng->h_ids.clear();
     std::fill(eng->index_of.begin(), eng->index_of.end(), 0xFFFFFFFFu);
-    mirror_append(eng, lits.data(), off.data(), (int64_t) ids.size(), ids.data());
+    mirror_append(eng, lits.data(), off.data(), (int64_t) ids.size(), ids.data(), eng->max_var);
     eng->next_id = next;
     return upload_all(eng);
 }
+
+int gss_db_set_locality(gss_engine *eng, int range_log2) {
+    if (!eng) return set_error(GSS_ERR_INVALID, "engine is NULL");
+    if (range_log2 != -1 && range_log2 != 0 && (range_log2 < 11 || range_log2 > 31))
+        return set_error(GSS_ERR_INVALID, "range_log2 must be -1 (automatic), 0 (off) or 11..31, not %d", range_log2);
+    eng->range_log2 = range_log2;
+    return GSS_OK;
+}
+
+int gss_db_locality_shift(const gss_engine *eng) { return eng ? effective_range_shift(eng, eng->max_var) : -1; }
 
 int64_t gss_db_live_count(const gss_engine *eng) { return eng ? eng->n_clauses - eng->n_dead : -1; }
 

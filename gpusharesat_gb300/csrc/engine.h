@@ -41,6 +41,9 @@ struct gss_engine {
     bool alive_dirty = false;
     int64_t n_dead = 0;
     uint32_t next_id = 0;
+    // variable ranges of the database order (gss_db_set_locality): log2 of
+    // the variables per range, -1 automatic, 0 length order only
+    int range_log2 = -1;
 
     // kernel variant: kind (GSS_KERNEL_*), lanes (words) per clause (0 = pick
     // from the word count), loads in flight / clause slots, cache hints

@@ -70,6 +70,13 @@ typedef struct gss_engine gss_engine;
 const char *gss_last_error(void);
 /* Version string of the library, e.g. "gpusharesat-gb300 0.1 sm_103a". */
 const char *gss_version(void);
+/* Testing hook, no counterpart in the reference: the next `count` device
+ * allocations of at least min_bytes made by the library fail as if the GPU
+ * were out of memory (the failure is made on the host; nothing reaches the
+ * device). It exercises the out-of-memory recovery of gss_sharer_gpu_run,
+ * which follows GpuRunner::wholeRun's notEnoughGpuMemory path
+ * (gpuShareLib/GpuRunner.cu:243-260). count = 0 turns it off. Process-wide. */
+int gss_debug_fail_device_alloc(int64_t min_bytes, int count);
 
 /* ---- engine lifetime ---- */
 /* Creates an engine on CUDA device `device`. Allocates nothing large yet. */
@@ -148,8 +155,22 @@ int gss_db_append(gss_engine *eng, const int32_t *lits, const int64_t *offsets, 
  * clause); their space is reclaimed by gss_db_compact. Unknown ids are
  * skipped and reported as GSS_ERR_NOT_FOUND after the known ones are removed. */
 int gss_db_delete(gss_engine *eng, const uint32_t *ids, int64_t n);
-/* Rewrites the database without the removed clauses (sorted by length again). */
+/* Rewrites the database without the removed clauses (in database order again). */
 int gss_db_compact(gss_engine *eng);
+/* Database order. The reference keeps clauses in per-size buckets
+ * (gpuShareLib/Clauses.cu:47-51); here the variables are also cut into ranges
+ * of 2^range_log2: each clause's literals are reordered so that those in its
+ * most frequent range come first, then those of its second range, and so on,
+ * and the clauses are ordered by (first range, second range, length). Warps
+ * that run side by side then gather the state rows of one or two ranges, a
+ * working set that stays in L2. Reports do not change (the rule does not
+ * depend on literal order). range_log2: -1 automatic (2^17 variables per
+ * range), 0 length order only, 11..31. Applies from the next gss_db_set,
+ * gss_db_append or gss_db_compact. */
+int gss_db_set_locality(gss_engine *eng, int range_log2);
+/* log2 of the variables per range of the current database order (0: length
+ * order only). */
+int gss_db_locality_shift(const gss_engine *eng);
 /* Clauses in the database, removed ones included until a compaction. */
 int64_t gss_db_clause_count(const gss_engine *eng);
 /* Clauses that take part in passes. */
@@ -222,6 +243,20 @@ int gss_check_passes_host(gss_engine *eng, int n_passes, const uint32_t *const *
  * assignment words in the wide layout, state[n_blocks][n_vars][32][2] =
  * {isDef, isTrue} for words 32*b .. 32*b + 31 (pad past the last word with
  * zeros), start[n_blocks * 32] and solver_of_word[n_blocks * 32].
+ * Preconditions. The inputs are in device memory, so the call cannot check
+ * them; the engine (gss_db_set, gss_check_launch) checks the same ones and
+ * refuses what breaks them. Here breaking one gives wrong reports or reads
+ * outside the buffers:
+ *   - every literal is 2*var + sign with 0 <= var < n_vars;
+ *   - every clause has 1 .. gss_max_clause_len() literals
+ *     (offsets[c] < offsets[c + 1]; an empty clause reports every started
+ *     slot);
+ *   - offsets[0] == 0 and offsets[n_clauses] < 2^31 (offsets are read as
+ *     32-bit positions);
+ *   - start[] and solver_of_word[] hold n_blocks * 32 entries, start zero
+ *     past the last real word (a padding word with start bits set reports).
+ * The call itself refuses n_parts outside 1..64, n_clauses > 0 with
+ * n_vars == 0, NULL pointers and an output capacity above 2^32 records.
  * Outputs: out[n_parts * cap_per_part] report records, partition p holding
  * min(counts_out[p], cap_per_part) records from out + p * cap_per_part, with
  * `clause` the CSR index; counts_out[n_parts]. A count above cap_per_part
@@ -230,8 +265,11 @@ int gss_check_passes_host(gss_engine *eng, int n_passes, const uint32_t *const *
  * 256-byte device array, which every GPU that loads this library keeps until
  * the process exits, and which all calls share: overlapping calls on the GPU
  * race and give wrong counts. Each call clears the counters first (they keep
- * the previous call's values). The first call on a device looks up the
- * array's device address; make that first call before any stream capture.
+ * the previous call's values). Each call looks up the array's device address
+ * on the current device (a host-side lookup that allocates nothing, so the
+ * address stays right after a cudaDeviceReset); the first call on a device
+ * also loads the library's device code there, so make that first call
+ * before any stream capture.
  * The results are the same as gss_check_launch's with the GSS_KERNEL_WIDE4
  * variant (8 lanes per clause, depth 2). */
 int gss_check_noalloc(const int32_t *lits, const int64_t *offsets, uint32_t n_clauses, const uint32_t *state,

@@ -45,6 +45,11 @@ def _lib():
         lib.oracle_check_one.argtypes = [
             ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
         ]
+        lib.oracle_check_digest.restype = ctypes.c_int
+        lib.oracle_check_digest.argtypes = [
+            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+            ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+        ]
         _LIB = lib
     return _LIB
 
@@ -100,3 +105,47 @@ def expand(reports):
                     slots.astype(np.int64)], axis=1)
     order = np.lexsort((out[:, 2], out[:, 1], out[:, 0]))
     return out[order]
+
+
+def check_digest(lits, offsets, state, start_mask, ids=None, n_threads=1):
+    """(record count, digest) of the oracle's reports, for passes too large to
+    compare record by record: the digest is the wrapping uint64 sum over
+    (clause, word, mask) records of mix(mix((id << 32) | word) ^ mask), mix =
+    the SplitMix64 finaliser, id = ids[clause] (the clause index when ids is
+    None). It does not depend on record order; report_digest() computes the
+    same from any report array."""
+    lits = np.ascontiguousarray(lits, dtype=np.int32)
+    offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+    state = np.ascontiguousarray(state, dtype=np.uint32)
+    start_mask = np.ascontiguousarray(start_mask, dtype=np.uint32)
+    ids_a = None if ids is None else np.ascontiguousarray(ids, dtype=np.uint32)
+    count = ctypes.c_uint64()
+    digest = ctypes.c_uint64()
+    rc = _lib().oracle_check_digest(_ptr(lits), _ptr(offsets), offsets.shape[0] - 1,
+                                    None if ids_a is None else _ptr(ids_a), _ptr(state), state.shape[1],
+                                    _ptr(start_mask), int(n_threads), ctypes.byref(count), ctypes.byref(digest))
+    if rc != 0:
+        raise RuntimeError("oracle_check_digest failed")
+    return int(count.value), int(digest.value)
+
+
+def _mix64(z):
+    z = z + np.uint64(0x9E3779B97F4A7C15)
+    z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+    z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    return z ^ (z >> np.uint64(31))
+
+
+def report_digest(clause, word, mask, chunk=1 << 25):
+    """(record count, digest) of report records given as arrays of clause ids,
+    words and masks, in any order (see check_digest)."""
+    n = int(len(clause))
+    total = np.uint64(0)
+    with np.errstate(over="ignore"):
+        for b in range(0, n, chunk):
+            c = np.asarray(clause[b:b + chunk]).astype(np.uint64)
+            w = np.asarray(word[b:b + chunk]).astype(np.uint64)
+            m = np.asarray(mask[b:b + chunk]).astype(np.uint64)
+            h = _mix64(_mix64((c << np.uint64(32)) | w) ^ m)
+            total = total + np.add.reduce(h, dtype=np.uint64)
+    return n, int(total)

@@ -199,3 +199,86 @@ uint32_t oracle_check_one(const int32_t *lits, int64_t len, const uint32_t *is_d
     }
     return all_false | one_undef;
 }
+
+/* ---- order-independent digest of a report set ----
+ *
+ * For passes too large to compare record by record in a test (hundreds of
+ * millions of records), the checker compares the number of (clause, word)
+ * records and the wrapping sum over records of
+ *     mix(mix((id << 32) | word) ^ mask)
+ * where id is the clause's id (ids[c], or c when ids is NULL) and mix is the
+ * SplitMix64 finaliser (Steele, Lea and Flood, "Fast splittable pseudorandom
+ * number generators", OOPSLA 2014). The sum does not depend on record order,
+ * so it can be computed the same way from the GPU's unordered output. */
+static inline uint64_t mix64(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+typedef struct {
+    const int32_t *lits;
+    const int64_t *offsets;
+    const uint32_t *ids;
+    int64_t c_begin, c_end;
+    const uint32_t *state;
+    int n_words;
+    const uint32_t *start_mask;
+    uint64_t count, digest;
+} digest_job;
+
+static void *digest_worker(void *arg) {
+    digest_job *j = (digest_job *) arg;
+    uint64_t count = 0, digest = 0;
+    for (int64_t c = j->c_begin; c < j->c_end; c++) {
+        const int32_t *cl = j->lits + j->offsets[c];
+        int64_t len = j->offsets[c + 1] - j->offsets[c];
+        uint64_t id = j->ids ? j->ids[c] : (uint64_t) c;
+        for (int w0 = 0; w0 < j->n_words; w0 += 2) {
+            uint64_t start = j->start_mask[w0];
+            if (w0 + 1 < j->n_words) start |= (uint64_t) j->start_mask[w0 + 1] << 32;
+            if (start == 0) continue;
+            uint64_t rep = check_pair(cl, len, j->state, j->n_words, w0, start);
+            for (int half = 0; half < 2 && rep; half++) {
+                uint32_t m = (uint32_t) (rep >> (32 * half));
+                if (m == 0) continue;
+                count++;
+                digest += mix64(mix64((id << 32) | (uint64_t) (w0 + half)) ^ (uint64_t) m);
+            }
+        }
+    }
+    j->count = count;
+    j->digest = digest;
+    return NULL;
+}
+
+/* Count and digest of the reports of every clause against every started
+ * slot (see above). Returns 0, or -1 on a bad argument. */
+int oracle_check_digest(const int32_t *lits, const int64_t *offsets, int64_t n_clauses, const uint32_t *ids,
+                        const uint32_t *state, int n_words, const uint32_t *start_mask, int n_threads,
+                        uint64_t *count, uint64_t *digest) {
+    if (n_clauses < 0 || n_words < 0 || !count || !digest) return -1;
+    *count = 0;
+    *digest = 0;
+    if (n_clauses == 0 || n_words == 0) return 0;
+    if (n_threads < 1) n_threads = 1;
+    if (n_threads > 256) n_threads = 256;
+    digest_job jobs[256];
+    pthread_t tids[256];
+    int64_t per = (n_clauses + n_threads - 1) / n_threads;
+    for (int t = 0; t < n_threads; t++) {
+        int64_t b = (int64_t) t * per, e = b + per;
+        if (b > n_clauses) b = n_clauses;
+        if (e > n_clauses) e = n_clauses;
+        jobs[t] = (digest_job){lits, offsets, ids, b, e, state, n_words, start_mask, 0, 0};
+    }
+    for (int t = 1; t < n_threads; t++) pthread_create(&tids[t], NULL, digest_worker, &jobs[t]);
+    digest_worker(&jobs[0]);
+    for (int t = 1; t < n_threads; t++) pthread_join(tids[t], NULL);
+    for (int t = 0; t < n_threads; t++) {
+        *count += jobs[t].count;
+        *digest += jobs[t].digest;
+    }
+    return 0;
+}

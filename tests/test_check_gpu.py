@@ -192,12 +192,14 @@ PIPELINED_VARIANTS = [(kind, l, d, 4 | occ * 2) for kind, l, ds in ((2, 8, (1, 2
                       for d in ds for occ in (0, 1)]
 
 
+@pytest.mark.parametrize("locality", [0, 11])
 @pytest.mark.parametrize("kind,lpc,depth,hints",
                          DIRECT_VARIANTS + TILED_VARIANTS + WIDE_VARIANTS + PIPELINED_VARIANTS + PERSISTENT_VARIANTS)
-def test_every_kernel_variant_matches_oracle(engine, kind, lpc, depth, hints):
+def test_every_kernel_variant_matches_oracle(engine, kind, lpc, depth, hints, locality):
     """Each kernel variant (kind, lanes per clause, loads in flight or clause
     slots, cache hints) is bit-exact, including slot counts that do not fill
-    the last slot block and clauses longer than a tile."""
+    the last slot block and clauses longer than a tile, in length order and
+    in variable-range order (8 ranges of 2^11 variables)."""
     wl = W.make_scale(seed=11, n_vars=2 ** 14, n_clauses=20_000, n_solvers=13)
     # a few clauses longer than a staged tile (512 literals)
     rng = np.random.default_rng(5)
@@ -207,10 +209,13 @@ def test_every_kernel_variant_matches_oracle(engine, kind, lpc, depth, hints):
     wl = W.Workload(wl.name, wl.n_vars, lits, offsets, wl.state, wl.start, wl.solver_of_word, wl.n_solvers)
     ref = oracle.check(wl.lits, wl.offsets, wl.state, wl.start)
     engine.set_variant(kind, lpc, depth, hints)
+    engine.set_locality(locality)
     try:
         gpu = _gpu_reports(engine, wl)
+        assert engine.locality_shift == locality
     finally:
         engine.set_variant()
+        engine.set_locality(-1)
     _assert_same(gpu, ref, wl)
 
 
@@ -225,15 +230,18 @@ def _live_reference(live, state, start):
     return np.sort(ref, order=["clause", "word"])
 
 
+@pytest.mark.parametrize("locality", [0, 11])
 @pytest.mark.parametrize("kind", [-1, 0, 2])
-def test_database_churn_matches_oracle(engine, kind):
+def test_database_churn_matches_oracle(engine, kind, locality):
     """Deletes (tombstones), appends with ids, and a compaction: every pass
-    reports exactly the live clauses' reports, keyed by clause id."""
+    reports exactly the live clauses' reports, keyed by clause id, in length
+    order and in variable-range order (2 ranges of 2^11 variables)."""
     import gpusharesat_gb300 as g
     rng = np.random.default_rng(31)
     base = W.make_scale(seed=31, n_vars=2 ** 12, n_clauses=20000, n_solvers=32)
     live = {c: base.lits[base.offsets[c]:base.offsets[c + 1]].tolist() for c in range(base.n_clauses)}
     engine.set_variant(kind, 0, 2, 0)
+    engine.set_locality(locality)
     engine.set_db(base.lits, base.offsets)
     engine.set_state(base.state, base.start, base.solver_of_word)
     next_id = base.n_clauses
@@ -261,6 +269,7 @@ def test_database_churn_matches_oracle(engine, kind):
     with pytest.raises(g.GssError):
         engine.delete([10 ** 8])
     engine.set_variant()
+    engine.set_locality(-1)
 
 
 def test_persistent_graph_replays_across_passes(engine):
@@ -304,9 +313,10 @@ def test_persistent_graph_replays_across_passes(engine):
 
 # ---- the bucketed kernel: a lane layout per length class ----
 
-def _plan_engine(wl):
+def _plan_engine(wl, locality=-1):
     import gpusharesat_gb300 as g
     eng = g.Engine(0)
+    eng.set_locality(locality)
     eng.set_db(wl.lits, wl.offsets)
     eng.set_variant(g.KERNEL_WIDE4, 8, 2, g.VARIANT_PERSISTENT)
     eng.set_state(wl.state, wl.start, wl.solver_of_word)
@@ -323,7 +333,7 @@ def test_length_plan_matches_oracle(lib, seed):
     wl = W.make_scale(seed=40 + seed, n_vars=2 ** 13, n_clauses=30000, n_solvers=n_solvers)
     if seed == 2:  # two words per solver, as the batching workload
         wl = W.make_batching(seed=42, n_vars=2 ** 13, n_clauses=30000, n_solvers=48)
-    eng = _plan_engine(wl)
+    eng = _plan_engine(wl, locality=11 if seed else 0)  # variable ranges: 4 ranges of 2^11
     ref = oracle.check(wl.lits, wl.offsets, wl.state, wl.start)
     for _ in range(3):
         layouts = rng.choice(g.LAYOUTS, size=4).tolist()
@@ -354,7 +364,7 @@ def test_length_plan_with_churn_and_graph(lib):
     rng = np.random.default_rng(45)
     base = W.make_scale(seed=45, n_vars=2 ** 12, n_clauses=20000, n_solvers=32)
     live = {c: base.lits[base.offsets[c]:base.offsets[c + 1]].tolist() for c in range(base.n_clauses)}
-    eng = _plan_engine(base)
+    eng = _plan_engine(base, locality=11)  # 2 ranges of 2^11 variables: a run per (range pair, class)
     eng.set_graph(True)
     eng.set_length_plan((3, 8, 20, 1 << 30), [g.LAYOUT_1x32_G2, g.LAYOUT_2x16_G1, g.LAYOUT_4x8_G2, g.LAYOUT_4x8_G1])
     next_id = base.n_clauses

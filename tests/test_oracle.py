@@ -58,3 +58,22 @@ def test_unstarted_slots_are_ignored(oracle_lib):
     state = np.zeros((1, 1, 2), np.uint32)  # undefined everywhere: a unit reports
     got = oracle.check(lits, offsets, state, np.array([0x5], np.uint32))
     assert len(got) == 1 and got["mask"][0] == 0x5
+
+
+def test_digest_matches_records_and_sees_a_changed_record(oracle_lib):
+    """The order-independent digest the full-size GPU tests compare: the
+    oracle's in-C digest equals the digest of its own records (in any order,
+    with clause ids mapped), and one changed record changes it."""
+    wl = W.make_small(seed=3, n_clauses=20000)
+    ref = oracle.check(wl.lits, wl.offsets, wl.state, wl.start, n_threads=4)
+    ids = (np.arange(wl.n_clauses, dtype=np.uint32) * 7 + 3).astype(np.uint32)
+    want = oracle.check_digest(wl.lits, wl.offsets, wl.state, wl.start, ids=ids, n_threads=3)
+    perm = np.random.default_rng(0).permutation(len(ref))
+    shuffled = ref[perm]
+    assert oracle.report_digest(ids[shuffled["clause"]], shuffled["word"], shuffled["mask"]) == want
+    assert want[0] == len(ref)
+    bad = shuffled.copy()
+    bad["mask"][5] ^= np.uint32(1 << 7)
+    assert oracle.report_digest(ids[bad["clause"]], bad["word"], bad["mask"]) != want
+    assert oracle.check_digest(wl.lits, wl.offsets, wl.state, wl.start, n_threads=1) == \
+        oracle.report_digest(ref["clause"], ref["word"], ref["mask"])
