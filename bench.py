@@ -62,6 +62,8 @@ def parse():
     p.add_argument("--locality", type=int, default=-1,
                    help="database order: -1 automatic variable ranges, 0 length order, 11..31 ranges of 2^n vars")
     p.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
+    p.add_argument("--serving-seconds", type=float, default=3.0,
+                   help="measured seconds per rate of the serving leg (0: skip it)")
     return p.parse_args()
 
 
@@ -195,6 +197,35 @@ def max_over_ranks(value, world, device):
 def job_throughput(units_per_rank_per_step, world, max_seconds_per_step):
     """Whole-job units/s: all ranks' units over the slowest rank's time."""
     return units_per_rank_per_step * world / max_seconds_per_step
+
+
+SERVING_RATES = (5e4, 1e5, 2e5)
+
+
+def serving_leg(seconds):
+    """Submit-to-report latency through the GpuClauseSharer C ABI
+    (gss_sharer_*: addClause, trySendAssignment, gpuRun, popReportedClause,
+    getLastAssigAllReported), driven by the C++ load generator
+    gss_serving_run in the serving shape: 2^21 variables, a 16e6-clause HBM
+    budget filled at the start, a clause stream of 2e5 clauses/s with
+    oldest-unreported eviction, 64 solver threads sending Poisson batches of
+    1..32 assignments at an aggregate 5e4, 1e5 and 2e5 assignments/s, 0.05%
+    planted reports. Latency of an assignment: its arrival (batch time) to
+    the moment getLastAssigAllReported passes it for its solver."""
+    import gpusharesat_gb300 as g
+    rows = []
+    for rate in SERVING_RATES:
+        r = g.serving_run(seconds=seconds, warmup_seconds=1.0, assign_rate=rate, n_solvers=64, n_vars=2 ** 21,
+                          budget=16_000_000, initial_clauses=16_000_000, clause_rate=2e5, plant_rate=0.0005,
+                          batch_max=32, trail_fraction=0.5, trail_change=8, seed=3)
+        rows.append({"rate_assignments_per_s": rate, "p50_ms": r["p50_ms"], "p99_ms": r["p99_ms"],
+                     "p999_ms": r["p999_ms"], "mean_ms": r["mean_ms"], "assignments": r["assignments"],
+                     "checks_per_s": r["checks_per_s"], "passes": r["passes"], "retries": r["retries"],
+                     "evicted": r["evicted"]})
+    return {"endpoints": "trySendAssignment arrival -> getLastAssigAllReported (GpuClauseSharer.h:151)",
+            "workload": "2^21 variables, 16e6-clause budget, 2e5 clauses/s stream, 64 solvers, batches of 1-32, "
+                        "0.05%% planted reports, %.0f s measured per rate after 1 s warm-up" % seconds,
+            "rates": rows}
 
 
 def cpu_parity(wl, gpu_reports, threads=None):
@@ -401,6 +432,8 @@ def run_gpu(args):
             "gpu_launches": gpu_launches,
             "clocks": clocks,
         }
+        if args.serving_seconds > 0 and args.workload == "scale":
+            line["latency"] = serving_leg(args.serving_seconds)
         if not args.no_cpu_baseline:
             line["parity"] = cpu_parity(wl, sizing_reports)
             v, cores, sample = cpu_baseline(wl, args.cpu_seconds)

@@ -143,6 +143,20 @@ struct CompactArgs {
     void *scratch;           // compact_scratch_bytes(n_clauses), 256-byte aligned
 };
 size_t compact_scratch_bytes(uint32_t n_clauses);
+// Rebuilds a CSR clause database in a new order on the device: new clause c
+// is old clause src[c], placed at new_offsets[c] (device arrays, n_new + 1
+// offsets); new_ids[c] = c; kClausePad zero literals after the last one.
+struct GatherArgs {
+    const int32_t *lits;
+    const int64_t *offsets;
+    const uint32_t *src;
+    const int64_t *new_offsets;
+    uint32_t n_new;
+    int64_t n_new_lits;
+    int32_t *new_lits;     // room for n_new_lits + kClausePad
+    uint32_t *new_ids;     // room for n_new
+};
+int gather_clauses(const GatherArgs &a, cudaStream_t stream, int sm_count);
 // Synchronizes `stream`; returns the live clause and literal counts.
 int compact_by_id(const CompactArgs &a, cudaStream_t stream, int sm_count, uint32_t *n_out, int64_t *lits_out);
 

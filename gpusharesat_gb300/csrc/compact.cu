@@ -7,6 +7,10 @@
 // clauses keep their order, their literals move to a second buffer, and the
 // id map follows. HBM-bound: every literal is read once and written once.
 //
+// gather_clauses rebuilds a database in a new order chosen on the host (a
+// reduceDb): the host sends, per kept clause, its old position and its new
+// offset (12 bytes); the literals move on the device.
+//
 // Four launches:
 //   1. per tile of kTileClauses clauses: live clause count and literal count
 //   2. one block: exclusive scan of the tile totals, the final offset and the
@@ -167,7 +171,38 @@ __global__ void copy_kernel(const int32_t *lits, const int64_t *offsets, const u
     }
 }
 
+// A warp per clause of the new database copies clause src[c]'s literals;
+// its lane 0 writes the clause's id (its new position).
+__global__ void gather_kernel(const int32_t *__restrict__ lits, const int64_t *__restrict__ offsets,
+                              const uint32_t *__restrict__ src, const int64_t *__restrict__ new_offsets, uint32_t n,
+                              int32_t *__restrict__ new_lits, uint32_t *__restrict__ new_ids) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < n; c += warps) {
+        const int64_t from = __ldg(offsets + __ldg(src + c));
+        const int64_t to = __ldg(new_offsets + c);
+        const int64_t len = __ldg(new_offsets + c + 1) - to;
+        for (int64_t i = lane; i < len; i += 32) new_lits[to + i] = __ldg(lits + from + i);
+        if (lane == 0) new_ids[c] = c;
+    }
+}
+
+__global__ void pad_kernel(int32_t *new_lits, int64_t n_lits) {
+    if (threadIdx.x < kClausePad) new_lits[n_lits + threadIdx.x] = 0;
+}
+
 }  // namespace
+
+int gather_clauses(const GatherArgs &a, cudaStream_t stream, int sm_count) {
+    if (a.n_new > 0) {
+        gather_kernel<<<(unsigned) std::max(sm_count, 1) * 8, 256, 0, stream>>>(a.lits, a.offsets, a.src, a.new_offsets,
+                                                                                a.n_new, a.new_lits, a.new_ids);
+        GSS_CUDA_TRY(cudaGetLastError());
+    }
+    pad_kernel<<<1, 32, 0, stream>>>(a.new_lits, a.n_new_lits);
+    GSS_CUDA_TRY(cudaGetLastError());
+    return GSS_OK;
+}
 
 size_t compact_scratch_bytes(uint32_t n_clauses) {
     const size_t tiles = ((size_t) n_clauses + kTileClauses - 1) / kTileClauses;

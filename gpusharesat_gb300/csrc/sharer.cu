@@ -191,7 +191,12 @@ Sharer::~Sharer() {
         cudaStreamSynchronize(stream_);
         cudaStreamDestroy(stream_);
     }
-    if (done_) cudaEventDestroy(done_);
+    for (Pass &p : pass_) {
+        if (p.counted) cudaEventDestroy(p.counted);
+        if (p.copied) cudaEventDestroy(p.copied);
+    }
+    if (alive_staged_) cudaEventDestroy(alive_staged_);
+    if (append_staged_) cudaEventDestroy(append_staged_);
 }
 
 void Sharer::log(int level, const std::string &msg) const {
@@ -221,10 +226,15 @@ int Sharer::init(int device) {
     }
     if (opt_.threads_per_block < 0) opt_.threads_per_block = 512;
     GSS_CUDA_TRY(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
-    GSS_CUDA_TRY(cudaEventCreateWithFlags(&done_, cudaEventDisableTiming));
-    GSS_TRY(d_counts_.reserve(sizeof(uint32_t) * n_parts_));
+    for (Pass &p : pass_) {
+        GSS_CUDA_TRY(cudaEventCreateWithFlags(&p.counted, cudaEventDisableTiming));
+        GSS_CUDA_TRY(cudaEventCreateWithFlags(&p.copied, cudaEventDisableTiming));
+        GSS_TRY(p.d_counts.reserve(sizeof(uint32_t) * n_parts_));
+        GSS_TRY(p.h_counts.reserve(sizeof(uint32_t) * (n_parts_ + 1)));
+    }
+    GSS_CUDA_TRY(cudaEventCreateWithFlags(&alive_staged_, cudaEventDisableTiming));
+    GSS_CUDA_TRY(cudaEventCreateWithFlags(&append_staged_, cudaEventDisableTiming));
     GSS_TRY(d_err_.reserve(sizeof(uint32_t)));
-    GSS_TRY(h_counts_.reserve(sizeof(uint32_t) * (n_parts_ + 1)));
     // one solver until told otherwise (HostAssigs constructor, Assigs.cu:311)
     return set_solver_count(1);
 }
@@ -529,6 +539,8 @@ int Sharer::upload_db() {
     GSS_CUDA_TRY(cudaStreamSynchronize(stream_));
     dev_clauses_ = n;
     dev_lits_ = offsets[n];
+    h_dev_meta_.resize(n);
+    for (uint32_t i = 0; i < n; i++) h_dev_meta_[i] = i;
     h_alive_.assign((n + 31) / 32, ~0u);
     n_dead_ = 0;
     dev_dead_ = 0;
@@ -559,9 +571,15 @@ int Sharer::sync_alive() {
     }
     alive_hi_ = std::min(alive_hi_, h_alive_.size());
     if (alive_lo_ < alive_hi_) {
-        GSS_CUDA_TRY(cudaMemcpyAsync((uint32_t *) d_alive_.ptr + alive_lo_, h_alive_.data() + alive_lo_,
-                                     (alive_hi_ - alive_lo_) * sizeof(uint32_t), cudaMemcpyHostToDevice, stream_));
-        GSS_CUDA_TRY(cudaStreamSynchronize(stream_));  // pageable source
+        // through pinned staging: a copy from pageable memory would wait for
+        // the whole stream (the pass in flight) first
+        const size_t bytes = (alive_hi_ - alive_lo_) * sizeof(uint32_t);
+        GSS_CUDA_TRY(cudaEventSynchronize(alive_staged_));  // the previous upload has left the stage
+        GSS_TRY(h_alive_stage_.reserve(bytes));
+        memcpy(h_alive_stage_.ptr, h_alive_.data() + alive_lo_, bytes);
+        GSS_CUDA_TRY(cudaMemcpyAsync((uint32_t *) d_alive_.ptr + alive_lo_, h_alive_stage_.ptr, bytes,
+                                     cudaMemcpyHostToDevice, stream_));
+        GSS_CUDA_TRY(cudaEventRecord(alive_staged_, stream_));
     }
     alive_synced_ = true;
     alive_lo_ = SIZE_MAX;
@@ -596,6 +614,14 @@ int Sharer::compact_device() {
         std::swap(bufs.first->ptr, bufs.second->ptr);
         std::swap(bufs.first->bytes, bufs.second->bytes);
     }
+    // the same order-preserving filter on the host's copy of the id map
+    size_t w = 0;
+    for (size_t p = 0; p < h_dev_meta_.size(); p++) {
+        const uint32_t i = h_dev_meta_[p];
+        if ((h_alive_[i >> 5] >> (i & 31)) & 1u) h_dev_meta_[w++] = i;
+    }
+    h_dev_meta_.resize(w);
+    if (w != kept) return set_error(GSS_ERR_STATE, "device compaction kept %u clauses, the host expects %zu", kept, w);
     dev_clauses_ = kept;
     dev_lits_ = kept_lits;
     dev_dead_ = 0;
@@ -646,16 +672,19 @@ void Sharer::evict(int64_t n) {
     }
 }
 
-int Sharer::compact(bool upload) {
+int Sharer::compact(bool upload, std::vector<uint32_t> *old_index) {
     // drops evicted clauses from meta_ and the activities, keeping the order
-    // (and so the age order); upload = rebuild the device database too
+    // (and so the age order); upload = rebuild the device database too;
+    // old_index receives the former index of each kept clause
     std::vector<uint8_t> keep(meta_.size(), 0);
     std::vector<ClauseMeta> kept;
     kept.reserve(meta_.size() - n_dead_);
+    if (old_index) old_index->clear();
     for (size_t i = 0; i < meta_.size(); i++) {
         if (h_alive_[i >> 5] & (1u << (i & 31))) {
             keep[i] = 1;
             kept.push_back(meta_[i]);
+            if (old_index) old_index->push_back((uint32_t) i);
         }
     }
     act_->compact(keep);
@@ -721,46 +750,80 @@ int Sharer::append_clauses(std::vector<int64_t> &ids, std::vector<int32_t> &lits
     new_lits.resize(off + kClausePad, 0);
     const uint32_t n = (uint32_t) meta_.size();
     const uint32_t n_dev = dpos + (uint32_t) ids.size();
+    // The host side is complete here: if the device side below runs out of
+    // memory, the caller rebuilds the device database from the host's.
+    h_alive_.resize((n + 31) / 32, 0u);
+    for (size_t i = first; i < n; i++) h_alive_[i >> 5] |= 1u << (i & 31);
+    mark_alive(first >> 5, h_alive_.size());
     if (end_off > 0x7FFFFF00LL) return set_error(GSS_ERR_NOMEM, "clause database exceeds 2^31 literals");
     // grow the device arrays, keeping their contents
     GSS_TRY(d_lits_.grow_keep((end_off + kClausePad) * sizeof(int32_t), stream_, base_off * sizeof(int32_t)));
     GSS_TRY(d_offsets_.grow_keep((n_dev + 1) * sizeof(int64_t), stream_, (dpos + 1) * sizeof(int64_t)));
     GSS_TRY(d_orig_.grow_keep(n_dev * sizeof(uint32_t), stream_, dpos * sizeof(uint32_t)));
-    std::vector<uint32_t> orig(ids.size());
-    for (size_t k = 0; k < ids.size(); k++) orig[k] = (uint32_t) (first + k);
-    GSS_CUDA_TRY(cudaMemcpyAsync((int32_t *) d_lits_.ptr + base_off, new_lits.data(), new_lits.size() * sizeof(int32_t),
-                                 cudaMemcpyHostToDevice, stream_));
-    if (dpos == 0) {
-        int64_t zero = 0;
-        GSS_CUDA_TRY(cudaMemcpyAsync(d_offsets_.ptr, &zero, sizeof(int64_t), cudaMemcpyHostToDevice, stream_));
+    // The batch goes up through one pinned stage (a copy from pageable
+    // memory would first wait for the whole stream, the pass in flight
+    // included): literals (+ zero padding), the offsets of the clause ends
+    // (after a leading zero when the database was empty), the ids.
+    const size_t nb = ids.size();
+    const size_t lit_bytes = new_lits.size() * sizeof(int32_t);
+    const size_t off_bytes = (nb + 1) * sizeof(int64_t);
+    const size_t lit_pad = (lit_bytes + 15) & ~(size_t) 15;
+    const size_t stage_bytes = lit_pad + off_bytes + nb * sizeof(uint32_t);
+    // A bulk load (the initial database, a large burst) goes up from pageable
+    // memory instead of growing the pinned stage past kMaxAppendStage; that
+    // copy waits for the stream, which a bulk load can afford.
+    constexpr size_t kMaxAppendStage = 64u << 20;
+    std::vector<char> bulk;
+    char *stage;
+    if (stage_bytes > kMaxAppendStage) {
+        bulk.resize(stage_bytes);
+        stage = bulk.data();
+    } else {
+        GSS_CUDA_TRY(cudaEventSynchronize(append_staged_));  // the previous batch has left the stage
+        GSS_TRY(h_append_.reserve(stage_bytes));
+        stage = (char *) h_append_.ptr;
     }
-    GSS_CUDA_TRY(cudaMemcpyAsync((int64_t *) d_offsets_.ptr + dpos + 1, new_offsets.data(),
-                                 new_offsets.size() * sizeof(int64_t), cudaMemcpyHostToDevice, stream_));
-    GSS_CUDA_TRY(cudaMemcpyAsync((uint32_t *) d_orig_.ptr + dpos, orig.data(), orig.size() * sizeof(uint32_t),
+    memcpy(stage, new_lits.data(), lit_bytes);
+    int64_t *st_off = (int64_t *) (stage + lit_pad);
+    st_off[0] = 0;
+    memcpy(st_off + 1, new_offsets.data(), nb * sizeof(int64_t));
+    uint32_t *st_orig = (uint32_t *) (stage + lit_pad + off_bytes);
+    for (size_t k = 0; k < nb; k++) st_orig[k] = (uint32_t) (first + k);
+    GSS_CUDA_TRY(cudaMemcpyAsync((int32_t *) d_lits_.ptr + base_off, stage, lit_bytes, cudaMemcpyHostToDevice,
+                                 stream_));
+    // offsets: [dpos] stays (or gets the leading zero), [dpos + 1 ..] are the new ends
+    if (dpos == 0)
+        GSS_CUDA_TRY(cudaMemcpyAsync(d_offsets_.ptr, st_off, off_bytes, cudaMemcpyHostToDevice, stream_));
+    else
+        GSS_CUDA_TRY(cudaMemcpyAsync((int64_t *) d_offsets_.ptr + dpos + 1, st_off + 1, nb * sizeof(int64_t),
+                                     cudaMemcpyHostToDevice, stream_));
+    GSS_CUDA_TRY(cudaMemcpyAsync((uint32_t *) d_orig_.ptr + dpos, st_orig, nb * sizeof(uint32_t),
                                  cudaMemcpyHostToDevice, stream_));
-    GSS_CUDA_TRY(cudaStreamSynchronize(stream_));  // the host vectors above are pageable
+    if (!bulk.empty()) {
+        GSS_CUDA_TRY(cudaStreamSynchronize(stream_));  // `bulk` is freed on return
+    } else {
+        GSS_CUDA_TRY(cudaEventRecord(append_staged_, stream_));
+    }
     dev_clauses_ = n_dev;
     dev_lits_ = end_off;
-    h_alive_.resize((n + 31) / 32, 0u);
-    for (size_t i = first; i < n; i++) h_alive_[i >> 5] |= 1u << (i & 31);
-    mark_alive(first >> 5, h_alive_.size());
+    h_dev_meta_.resize(n_dev);
+    for (size_t k = 0; k < nb; k++) h_dev_meta_[dpos + k] = (uint32_t) (first + k);
     return GSS_OK;
 }
 
 int Sharer::run_check(Pass &p) {
+    // start masks: p.h_start (pinned) holds n_blocks_ * bw_ words
     const size_t padded = (size_t) n_blocks_ * bw_;
-    std::vector<uint32_t> start(padded, 0u);
-    for (size_t w = 0; w < p.start.size() && w < padded; w++) start[w] = p.start[w];
-    GSS_CUDA_TRY(cudaMemcpyAsync(d_start_.ptr, start.data(), padded * sizeof(uint32_t), cudaMemcpyHostToDevice,
+    GSS_CUDA_TRY(cudaMemcpyAsync(d_start_.ptr, p.h_start.ptr, padded * sizeof(uint32_t), cudaMemcpyHostToDevice,
                                  stream_));
     // capacity: from the option (records per category x categories, as the
     // reference sizes its reporter) and what earlier passes needed
     const int64_t want = std::max<int64_t>((int64_t) opt_.init_report_count * opt_.block_count,
-                                           (int64_t) cap_per_part_ * n_parts_);
+                                           (int64_t) report_cap_ * n_parts_);
     const int64_t per = std::min<int64_t>((want + n_parts_ - 1) / n_parts_, 0x7FFFFFFF);
-    if ((uint32_t) per > cap_per_part_ || !d_reports_.ptr) {
-        GSS_TRY(d_reports_.reserve((size_t) per * n_parts_ * sizeof(gss_report)));
-        cap_per_part_ = (uint32_t) per;
+    if ((uint32_t) per > p.cap_per_part || !p.d_reports.ptr) {
+        GSS_TRY(p.d_reports.reserve((size_t) per * n_parts_ * sizeof(gss_report)));
+        p.cap_per_part = (uint32_t) per;
     }
     CheckArgs a;
     memset(&a, 0, sizeof a);
@@ -775,10 +838,10 @@ int Sharer::run_check(Pass &p) {
     a.n_blocks = (uint32_t) n_blocks_;
     a.start = (const uint32_t *) d_start_.ptr;
     a.solver_of_word = (const int32_t *) d_sow_.ptr;
-    a.out = (gss_report *) d_reports_.ptr;
-    a.counts = (uint32_t *) d_counts_.ptr;
+    a.out = (gss_report *) p.d_reports.ptr;
+    a.counts = (uint32_t *) p.d_counts.ptr;
     a.n_parts = n_parts_;
-    a.cap_per_part = cap_per_part_;
+    a.cap_per_part = p.cap_per_part;
     a.lpc = eff_lpc_;
     a.g = eff_depth_;
     a.cache_hints = (flags_ & GSS_VARIANT_L2_HINT) ? 1 : 0;
@@ -800,76 +863,97 @@ int Sharer::run_check(Pass &p) {
             GSS_TRY(launch_check(a, stream_, sm_count_));
         }
     }
-    GSS_CUDA_TRY(cudaMemcpyAsync(h_counts_.ptr, d_counts_.ptr, sizeof(uint32_t) * n_parts_, cudaMemcpyDeviceToHost,
+    GSS_CUDA_TRY(cudaMemcpyAsync(p.h_counts.ptr, p.d_counts.ptr, sizeof(uint32_t) * n_parts_, cudaMemcpyDeviceToHost,
                                  stream_));
-    GSS_CUDA_TRY(cudaMemcpyAsync((uint32_t *) h_counts_.ptr + n_parts_, d_err_.ptr, sizeof(uint32_t),
+    GSS_CUDA_TRY(cudaMemcpyAsync((uint32_t *) p.h_counts.ptr + n_parts_, d_err_.ptr, sizeof(uint32_t),
                                  cudaMemcpyDeviceToHost, stream_));
-    GSS_CUDA_TRY(cudaEventRecord(done_, stream_));
+    GSS_CUDA_TRY(cudaEventRecord(p.counted, stream_));
     return GSS_OK;
 }
 
-int Sharer::gather() {
-    // GpuRunner::gatherGpuRunResults (gpuShareLib/GpuRunner.cu:360-383)
-    Pass &p = pass_;
+int Sharer::collect(Pass &p) {
+    // GpuRunner::wholeRun waits for the check of the pass in flight
+    // (afterFindClauses, gpuShareLib/GpuRunner.cu:216-222), then queues the
+    // copy of its reports (scheduleGpuToCpuCopyAsync, :325-328) behind the
+    // set-to-last of its variables (launchGpu, :356-357).
     const int64_t t0 = now_us();
-    GSS_CUDA_TRY(cudaEventSynchronize(done_));
+    GSS_CUDA_TRY(cudaEventSynchronize(p.counted));
     if (opt_.quick_prof) stats_[kTimeSpentTestingClauses] += now_us() - t0;
     for (int attempt = 0;; attempt++) {
-        const uint32_t *hc = (const uint32_t *) h_counts_.ptr;
+        const uint32_t *hc = (const uint32_t *) p.h_counts.ptr;
         if (hc[n_parts_] != 0) return set_error(GSS_ERR_CUDA, "a bounded wait in the check kernel gave up");
         int64_t total = 0;
         bool overflow = false;
+        uint32_t most = 0;
         for (uint32_t q = 0; q < n_parts_; q++) {
             total += hc[q];
-            overflow |= hc[q] > cap_per_part_;
+            overflow |= hc[q] > p.cap_per_part;
+            most = std::max(most, hc[q]);
         }
         if (!overflow) {
-            h_reports_.resize((size_t) total);
+            p.n_reports = total;
+            GSS_TRY(p.h_reports.reserve(std::max<size_t>((size_t) total, 1) * sizeof(gss_report)));
             int64_t pos = 0;
             for (uint32_t q = 0; q < n_parts_; q++) {
                 if (!hc[q]) continue;
-                GSS_CUDA_TRY(cudaMemcpyAsync(h_reports_.data() + pos,
-                                             (gss_report *) d_reports_.ptr + (size_t) q * cap_per_part_,
+                GSS_CUDA_TRY(cudaMemcpyAsync((gss_report *) p.h_reports.ptr + pos,
+                                             (gss_report *) p.d_reports.ptr + (size_t) q * p.cap_per_part,
                                              hc[q] * sizeof(gss_report), cudaMemcpyDeviceToHost, stream_));
                 pos += hc[q];
             }
-            GSS_CUDA_TRY(cudaStreamSynchronize(stream_));
             break;
         }
         if (attempt >= 3) return set_error(GSS_ERR_OVERFLOW, "report queues kept overflowing");
-        // The pass's slots are still on the device (not broadcast yet): check again with room for all.
-        cap_per_part_ = 0;
-        const int64_t want = total * 2 + (int64_t) n_parts_ * 1024;
-        GSS_TRY(d_reports_.reserve((size_t) want * sizeof(gss_report)));
-        cap_per_part_ = (uint32_t) std::min<int64_t>(want / n_parts_, 0x7FFFFFFF);
+        // The pass's slots are still on the device (not broadcast yet): check
+        // again with room for all (for the later passes too).
+        report_cap_ = (uint32_t) std::min<int64_t>((int64_t) most * 2 + 1024, 0x7FFFFFFF);
         GSS_TRY(run_check(p));
-        GSS_CUDA_TRY(cudaEventSynchronize(done_));
+        GSS_CUDA_TRY(cudaEventSynchronize(p.counted));
     }
     // the pass's variables take their last slot's value in all 32 slots
+    // (stream-ordered: the next pass's updates are scattered after this)
     if (p.n_updates > 0) {
-        std::vector<uint32_t> last((size_t) n_blocks_ * bw_, 0u);
-        for (size_t w = 0; w < p.last_mask.size() && w < last.size(); w++) last[w] = p.last_mask[w];
-        GSS_CUDA_TRY(cudaMemcpyAsync(d_last_mask_.ptr, last.data(), last.size() * sizeof(uint32_t),
+        GSS_CUDA_TRY(cudaMemcpyAsync(d_last_mask_.ptr, p.h_last.ptr, (size_t) n_blocks_ * bw_ * sizeof(uint32_t),
                                      cudaMemcpyHostToDevice, stream_));
         set_to_last_kernel<<<grid_for(p.n_updates, sm_count_), 256, 0, stream_>>>(
             (const DevUpdate *) d_updates_.ptr, (uint32_t) p.n_updates, (const uint32_t *) d_last_mask_.ptr,
             (uint2 *) d_state_.ptr, (uint32_t) dev_vars_, (uint32_t) bw_);
         GSS_CUDA_TRY(cudaGetLastError());
-        GSS_CUDA_TRY(cudaStreamSynchronize(stream_));
     }
+    GSS_CUDA_TRY(cudaEventRecord(p.copied, stream_));
+    p.pending = false;
+    p.collected = true;
+    p.noted = false;
+    return GSS_OK;
+}
+
+int Sharer::note_reports(Pass &p) {
+    // The clause-side effects of a collected pass, cheap and needed before
+    // the next eviction: statistics, activity bumps and last-report passes
+    // (GpuRunner::gatherGpuRunResults, gpuShareLib/GpuRunner.cu:360-378).
+    if (!p.collected || p.noted) return GSS_OK;
+    GSS_CUDA_TRY(cudaEventSynchronize(p.copied));
+    const gss_report *rep = (const gss_report *) p.h_reports.ptr;
     stats_[kGpuRuns]++;
     stats_[kTotalAssigClauseTested] += (int64_t) p.n_clauses * p.assig_total;
     stats_[kClauseTestsOnGroups] += p.n_clauses;
     stats_[kClauseTestsOnAssigs] += (int64_t) p.n_clauses * p.active_words;
-    stats_[kGpuReports] += (int64_t) h_reports_.size();
-    for (const gss_report &r : h_reports_) {
-        act_->bump(r.clause);
-        meta_[r.clause].last_report = pass_no_;
+    stats_[kGpuReports] += p.n_reports;
+    for (int64_t i = 0; i < p.n_reports; i++) {
+        act_->bump(rep[i].clause);
+        meta_[rep[i].clause].last_report = p.number;
     }
-    pass_no_++;
-    const int64_t t1 = now_us();
+    p.noted = true;
+    return GSS_OK;
+}
+
+int Sharer::deliver(Pass &p) {
     // Reported::fill (gpuShareLib/Reported.cu:160-204): a batch for every
     // solver that had assignments in the pass, reported or not.
+    if (!p.collected) return GSS_OK;
+    GSS_TRY(note_reports(p));
+    const int64_t t1 = now_us();
+    const gss_report *rep = (const gss_report *) p.h_reports.ptr;
     std::vector<ClauseBatch *> batch(reported_.size(), nullptr);
     for (size_t s = 0; s < p.assig.size() && s < reported_.size(); s++) {
         if (p.assig[s].count > 0) {
@@ -877,7 +961,8 @@ int Sharer::gather() {
             batch[s]->assig = p.assig[s];
         }
     }
-    for (const gss_report &r : h_reports_) {
+    for (int64_t i = 0; i < p.n_reports; i++) {
+        const gss_report &r = rep[i];
         const int s = (int) r.solver;
         if (s < 0 || s >= (int) batch.size()) continue;
         if (!batch[s]) {
@@ -893,12 +978,25 @@ int Sharer::gather() {
     for (size_t s = 0; s < batch.size(); s++)
         if (batch[s]) reported_[s]->queue.publish();
     if (opt_.quick_prof) stats_[kTimeSpentFillingReported] += now_us() - t1;
-    p.pending = false;
+    p.collected = false;
     return GSS_OK;
 }
 
+int Sharer::finish_pending() {
+    // collects and delivers every pass (before a reduceDb renumbers clauses)
+    Pass &p = pass_[cur_];
+    if (p.pending) GSS_TRY(collect(p));
+    GSS_TRY(deliver(pass_[cur_ ^ 1]));
+    return deliver(p);
+}
+
 int Sharer::launch_pass() {
-    // GpuRunner::startGpuRunAsync (gpuShareLib/GpuRunner.cu:274-321)
+    // GpuRunner::startGpuRunAsync (gpuShareLib/GpuRunner.cu:274-321). The
+    // pass launched by the previous call (pass_[cur_]) is collected: its
+    // reports are on their way to the host and its set-to-last is queued.
+    Pass &prev = pass_[cur_];
+    Pass &p = pass_[cur_ ^ 1];
+    GSS_TRY(deliver(p));  // delivered by the previous call already; kept for safety
     std::vector<int64_t> ids;
     std::vector<int32_t> lits;
     std::vector<uint32_t> lens;
@@ -910,24 +1008,38 @@ int Sharer::launch_pass() {
     }
     if (!ids.empty()) {
         int rc = append_clauses(ids, lits, lens);
-        if (rc == GSS_ERR_NOMEM) out_of_memory_ = true;
+        if (rc == GSS_ERR_NOMEM) rc = recover_from_oom();
         GSS_TRY(rc);
     }
     if (budget_ > 0 && live_clauses() > budget_) {
+        // eviction keeps the recently reported clauses: it needs the
+        // collected pass's reports on the clauses first
+        GSS_TRY(note_reports(prev));
         evict(live_clauses() - budget_);
-        if (n_dead_ * 2 > (int64_t) meta_.size())
-            GSS_TRY(compact());  // host tombstones: rebuild everything
-        else if (dev_dead_ * 5 > (int64_t) dev_clauses_)
+        if (n_dead_ * 2 > (int64_t) meta_.size()) {
+            GSS_TRY(deliver(prev));  // a host compaction renumbers the clauses its reports name
+            GSS_TRY(compact());      // host tombstones: rebuild everything
+        } else if (dev_dead_ * 5 > (int64_t) dev_clauses_) {
             GSS_TRY(compact_device());
+        }
     }
     if (stats_[kGpuClauses] == 0) return GSS_OK;  // nothing to check: assignments wait
-    GSS_TRY(ensure_state());
+    int rc = ensure_state();
+    if (rc == GSS_ERR_NOMEM) {
+        GSS_TRY(recover_from_oom());
+        rc = ensure_state();
+    }
+    GSS_TRY(rc);
     const int64_t t0 = now_us();
-    Pass &p = pass_;
     const int n_solvers = (int) solvers_.size();
+    const size_t padded = (size_t) n_blocks_ * bw_;
+    GSS_TRY(p.h_start.reserve(padded * sizeof(uint32_t)));
+    GSS_TRY(p.h_last.reserve(padded * sizeof(uint32_t)));
+    uint32_t *start = (uint32_t *) p.h_start.ptr;
+    uint32_t *last = (uint32_t *) p.h_last.ptr;
+    memset(start, 0, padded * sizeof(uint32_t));
+    memset(last, 0, padded * sizeof(uint32_t));
     p.assig.assign(n_solvers, AssigIds());
-    p.start.assign(n_solvers, 0u);
-    p.last_mask.assign(n_solvers, 0u);
     p.assig_total = 0;
     p.active_words = 0;
     std::vector<DevUpdate> ups;
@@ -946,8 +1058,8 @@ int Sharer::launch_pass() {
             last_id = sa.current_id - 1;
         else
             last_id = sa.current_id;
-        p.start[s] = ~sa.not_completed;
-        p.last_mask[s] = 1u << (uint32_t) (last_id % kSlots);
+        start[s] = ~sa.not_completed;
+        last[s] = 1u << (uint32_t) (last_id % kSlots);
         for (const VarUpdate &u : sa.updates)
             if ((int) u.var < dev_vars_) ups.push_back(DevUpdate{u.var, (uint32_t) s, u.is_def, u.is_true});
         sa.updates.clear();
@@ -955,33 +1067,67 @@ int Sharer::launch_pass() {
         sa.not_completed = ~0u;
         sa.lock.unlock();
         p.assig_total += p.assig[s].count;
-        if (p.start[s]) p.active_words++;
+        if (start[s]) p.active_words++;
     }
     p.n_updates = (int64_t) ups.size();
-    if (!ups.empty()) {
-        const size_t bytes = ups.size() * sizeof(DevUpdate);
-        GSS_TRY(h_updates_.reserve(bytes));
-        GSS_TRY(d_updates_.reserve(bytes));
-        memcpy(h_updates_.ptr, ups.data(), bytes);
-        GSS_CUDA_TRY(cudaMemcpyAsync(d_updates_.ptr, h_updates_.ptr, bytes, cudaMemcpyHostToDevice, stream_));
-        scatter_updates_kernel<<<grid_for(ups.size(), sm_count_), 256, 0, stream_>>>(
-            (const DevUpdate *) d_updates_.ptr, (uint32_t) ups.size(), (uint2 *) d_state_.ptr, (uint32_t) dev_vars_,
-            (uint32_t) bw_);
-        GSS_CUDA_TRY(cudaGetLastError());
+    // The rings are cut: from here on the pass must run. If a device buffer
+    // cannot grow, the database is reduced and the same updates are sent
+    // again (GpuRunner::wholeRun, gpuShareLib/GpuRunner.cu:243-260).
+    auto send_and_check = [&]() -> int {
+        if (!ups.empty()) {
+            // h_updates_ is free: the previous pass's copy from it ran before
+            // that pass's check, which has finished
+            const size_t bytes = ups.size() * sizeof(DevUpdate);
+            GSS_TRY(d_updates_.reserve(bytes));
+            GSS_TRY(h_updates_.reserve(bytes));
+            memcpy(h_updates_.ptr, ups.data(), bytes);
+            GSS_CUDA_TRY(cudaMemcpyAsync(d_updates_.ptr, h_updates_.ptr, bytes, cudaMemcpyHostToDevice, stream_));
+            scatter_updates_kernel<<<grid_for(ups.size(), sm_count_), 256, 0, stream_>>>(
+                (const DevUpdate *) d_updates_.ptr, (uint32_t) ups.size(), (uint2 *) d_state_.ptr,
+                (uint32_t) dev_vars_, (uint32_t) bw_);
+            GSS_CUDA_TRY(cudaGetLastError());
+        }
+        p.n_clauses = dev_clauses_;
+        return run_check(p);
+    };
+    rc = send_and_check();
+    if (rc == GSS_ERR_NOMEM) {
+        GSS_TRY(recover_from_oom());
+        rc = send_and_check();
     }
+    GSS_TRY(rc);
     if (opt_.quick_prof) stats_[kTimeSpentFillingAssigs] += now_us() - t0;
-    p.n_clauses = dev_clauses_;
-    GSS_TRY(run_check(p));
     p.pending = true;
+    p.number = pass_no_++;
+    cur_ ^= 1;
     return GSS_OK;
 }
 
+int Sharer::recover_from_oom() {
+    // GpuRunner::wholeRun on notEnoughGpuMemory (gpuShareLib/GpuRunner.cu:243-260):
+    // reduce the clause database (HostClauses::reduceDb) and remember it
+    // (hasRunOutOfGpuMemoryOnce, which solvers read to stop growing their
+    // reduce period, glucose-syrup/gpu/GpuMultiSolver.cc:130-134). The
+    // reduced database is rebuilt on the device from the host's copy, whose
+    // old device buffers are freed first.
+    out_of_memory_ = true;
+    log(1, "c Ran out of GPU memory: reducing the GPU clause database\n");
+    GSS_TRY(finish_pending());
+    return reduce_now(false);  // an upload frees the old device buffers before allocating new ones
+}
+
 int Sharer::gpu_run() {
-    // GpuClauseSharerImpl::gpuRun (gpuShareLib/GpuClauseSharerImpl.cu:83-94)
+    // GpuClauseSharerImpl::gpuRun -> GpuRunner::wholeRun
+    // (gpuShareLib/GpuClauseSharerImpl.cu:83-94, GpuRunner.cu:211-261): the
+    // pass in flight is collected, the next one is cut and launched, and the
+    // collected pass's reports are delivered to the solvers' queues while the
+    // new one runs on the GPU.
     const int64_t t0 = now_us();
     GSS_CUDA_TRY(cudaSetDevice(device_));
-    if (pass_.pending) GSS_TRY(gather());
+    Pass &prev = pass_[cur_];
+    if (prev.pending) GSS_TRY(collect(prev));
     GSS_TRY(launch_pass());
+    GSS_TRY(deliver(prev));
     const int64_t spent = now_us() - t0;
     if (spent < opt_.min_latency_us) std::this_thread::sleep_for(std::chrono::microseconds(opt_.min_latency_us - spent));
     return GSS_OK;
@@ -994,8 +1140,23 @@ int Sharer::reduce_db() {
     // GpuClauseSharerImpl.cu:72): keep clauses of length 1 and 2, and longer
     // ones with lbd < 100 whose activity reaches the median estimate.
     GSS_CUDA_TRY(cudaSetDevice(device_));
-    if (pass_.pending) GSS_TRY(gather());
-    if (n_dead_ > 0) GSS_TRY(compact(false));  // the upload below rebuilds the device side
+    GSS_TRY(finish_pending());
+    return reduce_now(true);
+}
+
+int Sharer::reduce_now(bool on_device) {
+    // Where each clause is on the device now, by meta_ index (-1: not there,
+    // which happens only after a failed upload).
+    std::vector<int64_t> dev_pos(meta_.size(), -1);
+    if (h_dev_meta_.size() == dev_clauses_)
+        for (size_t p = 0; p < h_dev_meta_.size(); p++) dev_pos[h_dev_meta_[p]] = (int64_t) p;
+    std::vector<uint32_t> from_compact;  // meta_ index before the tombstones went
+    if (n_dead_ > 0) {
+        GSS_TRY(compact(false, &from_compact));  // the rebuild below replaces the device side
+    } else {
+        from_compact.resize(meta_.size());
+        for (size_t i = 0; i < meta_.size(); i++) from_compact[i] = (uint32_t) i;
+    }
     const int64_t t0 = now_us();
     added_at_last_reduce_ = stats_[kGpuClausesAdded];
     stats_[kGpuReduceDbs]++;
@@ -1010,6 +1171,7 @@ int Sharer::reduce_db() {
     // PerSizeKeeper::tryRemoveClausesAsync (Clauses.cu:249-282) only looks at
     // clauses of length 3 and more.
     std::vector<ClauseMeta> kept;
+    std::vector<uint32_t> kept_from;
     std::vector<uint8_t> keep(meta_.size(), 0);
     kept.reserve(meta_.size());
     int64_t len_sum = 0;
@@ -1019,6 +1181,7 @@ int Sharer::reduce_db() {
                                                max_lim, act)) {
             keep[i] = 1;
             kept.push_back(m);
+            kept_from.push_back(from_compact[i]);
             len_sum += m.len;
         }
     }
@@ -1026,18 +1189,84 @@ int Sharer::reduce_db() {
     std::vector<uint32_t> order(kept.size());
     for (uint32_t i = 0; i < order.size(); i++) order[i] = i;
     std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return kept[a].len < kept[b].len; });
-    meta_.resize(kept.size());
-    for (size_t k = 0; k < order.size(); k++) meta_[k] = kept[order[k]];
+    const uint32_t n = (uint32_t) kept.size();
+    meta_.resize(n);
+    std::vector<uint32_t> src(std::max<uint32_t>(n, 1));
+    bool all_on_device = on_device;
+    for (uint32_t k = 0; k < n; k++) {
+        meta_[k] = kept[order[k]];
+        const int64_t p = dev_pos[kept_from[order[k]]];
+        all_on_device &= p >= 0;
+        src[k] = (uint32_t) std::max<int64_t>(p, 0);
+    }
     act_->permute(order);
     stats_[kGpuClauses] = (int64_t) meta_.size();
     stats_[kGpuClauseLengthSum] = len_sum;
-    GSS_TRY(upload_db());
+    if (all_on_device) {
+        GSS_TRY(rebuild_on_device(src));
+    } else {
+        GSS_TRY(upload_db());
+    }
     stats_[kTimeSpentReduceGpuDb] += now_us() - t0;
     {
         std::ostringstream os;
         os << "c Done reducing gpu clause db, clause count is " << stats_[kGpuClauses];
         log(2, os.str());
     }
+    return GSS_OK;
+}
+
+int Sharer::rebuild_on_device(const std::vector<uint32_t> &src) {
+    // The device database in meta_ order, its literals moved on the device
+    // (gather_clauses): only the old position and the new offset of each
+    // clause go up, 12 bytes a clause, instead of all its literals.
+    const uint32_t n = (uint32_t) meta_.size();
+    std::vector<int64_t> offsets(n + 1, 0);
+    for (uint32_t i = 0; i < n; i++) offsets[i + 1] = offsets[i] + meta_[i].len;
+    const int64_t n_lits = offsets[n];
+    GSS_TRY(d_lits2_.reserve((size_t) (n_lits + kClausePad) * sizeof(int32_t)));
+    GSS_TRY(d_offsets2_.reserve(((size_t) n + 1) * sizeof(int64_t)));
+    GSS_TRY(d_orig2_.reserve(std::max<size_t>(n, 1) * sizeof(uint32_t)));
+    GSS_TRY(d_compact_.reserve(std::max<size_t>(n, 1) * sizeof(uint32_t)));
+    GSS_CUDA_TRY(cudaMemcpy(d_offsets2_.ptr, offsets.data(), ((size_t) n + 1) * sizeof(int64_t),
+                            cudaMemcpyHostToDevice));
+    GSS_CUDA_TRY(cudaMemcpy(d_compact_.ptr, src.data(), std::max<size_t>(n, 1) * sizeof(uint32_t),
+                            cudaMemcpyHostToDevice));
+    GatherArgs g;
+    g.lits = (const int32_t *) d_lits_.ptr;
+    g.offsets = (const int64_t *) d_offsets_.ptr;
+    g.src = (const uint32_t *) d_compact_.ptr;
+    g.new_offsets = (const int64_t *) d_offsets2_.ptr;
+    g.n_new = n;
+    g.n_new_lits = n_lits;
+    g.new_lits = (int32_t *) d_lits2_.ptr;
+    g.new_ids = (uint32_t *) d_orig2_.ptr;
+    GSS_TRY(gather_clauses(g, stream_, sm_count_));
+    GSS_CUDA_TRY(cudaStreamSynchronize(stream_));
+    for (auto bufs : {std::make_pair(&d_lits_, &d_lits2_), std::make_pair(&d_offsets_, &d_offsets2_),
+                      std::make_pair(&d_orig_, &d_orig2_)}) {
+        std::swap(bufs.first->ptr, bufs.second->ptr);
+        std::swap(bufs.first->bytes, bufs.second->bytes);
+    }
+    // the host arena in the new order too
+    std::vector<int32_t> arena((size_t) n_lits);
+    for (uint32_t i = 0; i < n; i++) {
+        memcpy(&arena[offsets[i]], &h_lits_[meta_[i].lit_off], meta_[i].len * sizeof(int32_t));
+        meta_[i].lit_off = (uint32_t) offsets[i];
+    }
+    h_lits_.swap(arena);
+    dev_clauses_ = n;
+    dev_lits_ = n_lits;
+    h_dev_meta_.resize(n);
+    for (uint32_t i = 0; i < n; i++) h_dev_meta_[i] = i;
+    h_alive_.assign((n + 31) / 32, ~0u);
+    n_dead_ = 0;
+    dev_dead_ = 0;
+    evict_cursor_ = 0;
+    alive_synced_ = false;
+    alive_lo_ = SIZE_MAX;
+    alive_hi_ = 0;
+    device_compactions_++;
     return GSS_OK;
 }
 

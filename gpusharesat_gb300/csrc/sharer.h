@@ -165,25 +165,42 @@ public:
     int64_t live_clauses() const { return (int64_t) meta_.size() - n_dead_; }
 
 private:
+    // One pass in flight or waiting for delivery. Two of them alternate, so
+    // the host delivers pass N's reports while the GPU checks pass N+1.
     struct Pass {
-        bool pending = false;
+        bool pending = false;    // launched, not collected
+        bool collected = false;  // counts read and reports copying to the host, not delivered
+        bool noted = false;      // its reports already marked on the clauses (last report, activity)
         std::vector<AssigIds> assig;
-        std::vector<uint32_t> start;
-        std::vector<uint32_t> last_mask;
         uint32_t n_clauses = 0;
         int64_t n_updates = 0;
         int64_t assig_total = 0;
         int active_words = 0;
+        int64_t n_reports = 0;
+        int32_t number = 0;      // pass_no_ at its launch
+        // device report queues and their counters, pinned host copies of the
+        // counters (+ error flag), the start and last-slot masks and the reports
+        DevBuf d_reports, d_counts;
+        uint32_t cap_per_part = 0;
+        PinnedBuf h_counts, h_start, h_last, h_reports;
+        cudaEvent_t counted = nullptr;  // counts copied to h_counts
+        cudaEvent_t copied = nullptr;   // reports copied to h_reports
     };
 
-    int gather();
+    int collect(Pass &p);
+    int note_reports(Pass &p);
+    int deliver(Pass &p);
+    int finish_pending();
+    int reduce_now(bool on_device);
+    int rebuild_on_device(const std::vector<uint32_t> &src);
+    int recover_from_oom();
     int launch_pass();
     int run_check(Pass &p);
     int ensure_state();
     int append_clauses(std::vector<int64_t> &ids, std::vector<int32_t> &lits, std::vector<uint32_t> &lens);
     int upload_db();
     void evict(int64_t n);
-    int compact(bool upload = true);
+    int compact(bool upload = true, std::vector<uint32_t> *old_index = nullptr);
     int compact_device();
     int sync_alive();
     void mark_alive(size_t lo_word, size_t hi_word);
@@ -194,7 +211,6 @@ private:
     std::function<void(const std::string &)> log_fn_;
     int device_ = 0, sm_count_ = 0;
     cudaStream_t stream_ = nullptr;
-    cudaEvent_t done_ = nullptr;
     int max_len_ = 100;  // MAX_CL_SIZE, gpuShareLib/BaseTypes.cuh:28
 
     // statistics
@@ -219,6 +235,7 @@ private:
     // order with evicted clauses compacted away.
     DevBuf d_lits_, d_offsets_, d_orig_;
     DevBuf d_lits2_, d_offsets2_, d_orig2_, d_compact_;  // compaction targets, swapped in
+    std::vector<uint32_t> h_dev_meta_;  // host copy of d_orig_: meta_ index of each device position
     int64_t dev_lits_ = 0;
     uint32_t dev_clauses_ = 0;
     int64_t max_var_ = -1;
@@ -233,9 +250,11 @@ private:
     int64_t n_dead_ = 0;     // tombstones in meta_
     int64_t dev_dead_ = 0;   // evicted clauses still in the device arrays
     size_t evict_cursor_ = 0;
-    int32_t pass_no_ = 0;
+    int32_t pass_no_ = 0;    // passes launched so far (the number of the next one)
     std::vector<uint32_t> h_alive_;  // bit per meta_ index
     DevBuf d_alive_;
+    PinnedBuf h_alive_stage_;        // staging of alive-bit uploads
+    cudaEvent_t alive_staged_ = nullptr;
     bool alive_synced_ = false;      // d_alive_ holds h_alive_ except [alive_lo_, alive_hi_)
     size_t alive_lo_ = SIZE_MAX, alive_hi_ = 0;
     int64_t device_compactions_ = 0;
@@ -246,16 +265,18 @@ private:
     std::vector<std::unique_ptr<SolverReported>> reported_;
     DevBuf d_state_, d_start_, d_sow_, d_updates_, d_last_mask_;
     PinnedBuf h_updates_;
+    PinnedBuf h_append_;             // staging of appended clauses (literals, offsets, ids)
+    cudaEvent_t append_staged_ = nullptr;
     int dev_vars_ = 0, dev_words_ = 0;
     int kind_ = GSS_KERNEL_AUTO, lpc_req_ = 0, depth_req_ = 2, flags_ = 0;
     int eff_kind_ = GSS_KERNEL_DIRECT, eff_lpc_ = 1, eff_depth_ = 2, bw_ = 1, n_blocks_ = 0;
 
-    // reports
-    DevBuf d_reports_, d_counts_, d_err_;
-    PinnedBuf h_counts_;
-    uint32_t n_parts_ = 16, cap_per_part_ = 0;
-    std::vector<gss_report> h_reports_;
-    Pass pass_;
+    // reports: two passes, alternating (the one launched last is pass_[cur_])
+    DevBuf d_err_;
+    uint32_t n_parts_ = 16;
+    uint32_t report_cap_ = 0;  // records per partition that earlier passes needed
+    Pass pass_[2];
+    int cur_ = 0;
 };
 
 }  // namespace gss

@@ -37,9 +37,10 @@ def test_dropin_runs_reference_known_answers(lib, tmp_path):
 # glucose-syrup/gpu/Makefile:9, rel-newtech/gpu/Makefile:9). gpuShareLib is
 # dropped from DEPDIR: its headers come from include/ (first on the include
 # path) and its code from libgpusharesat.so. The sources are read where they
-# lie in the reference tree (only present where the reference is checked
-# out; the outputs go to pytest's temporary directory).
-REFERENCE = os.environ.get("GPUSHARESAT_REFERENCE", "/root/reference")
+# lie in the reference tree, named by the GPUSHARESAT_REFERENCE environment
+# variable (the tests skip without it; the outputs go to pytest's temporary
+# directory).
+REFERENCE = os.environ.get("GPUSHARESAT_REFERENCE")
 SOLVERS = {
     "glucose-syrup": ["glucose-syrup/mtl", "glucose-syrup/utils", "glucose-syrup/core", "glucose-syrup/simp",
                       "glucose-syrup/satUtils"],
@@ -58,8 +59,8 @@ def _solver_sources(name):
 
 @pytest.mark.parametrize("name", sorted(SOLVERS))
 def test_reference_solver_builds_unchanged(lib, tmp_path, name):
-    if not os.path.isdir(os.path.join(REFERENCE, name, "gpu")):
-        pytest.skip("the reference's solver sources are not here")
+    if not REFERENCE or not os.path.isdir(os.path.join(REFERENCE, name, "gpu")):
+        pytest.skip("GPUSHARESAT_REFERENCE does not name a checkout of the reference's solver sources")
     from concurrent.futures import ThreadPoolExecutor
     srcs = _solver_sources(name)
     assert len(srcs) >= 10

@@ -198,7 +198,9 @@ def test_reduce_db_after_evictions(lib):
     assert s.trySetSolverValues(0, [lit(0)]) and s.trySendAssignment(0) >= 0
     execute(s)
     assert s.evictedCount() == 200 and s.getGlobalStat(GPU_CLAUSES) == 300
+    rebuilt = s.deviceCompactions()
     s.reduceDb()
+    assert s.deviceCompactions() == rebuilt + 1  # rebuilt on the device, evicted clauses dropped
     assert s.getGlobalStat(GPU_CLAUSES) == 300
     all_false(s, 1, n_vars)
     execute(s)

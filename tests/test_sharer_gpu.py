@@ -271,7 +271,10 @@ def test_reduce_db(lib):
     assert s.getGlobalStat("gpuClauses") == 2
     assert s.getGlobalStat("gpuClauseLengthSum") == 6
     t.enqueue(lit(2))  # the solver propagates the imported clause
+    rebuilt = s.deviceCompactions()
     s.reduceDb()
+    # the kept clause moved on the device (no re-upload of the database)
+    assert s.deviceCompactions() == rebuilt + 1
     assert s.getGlobalStat("gpuClauses") == 1
     assert s.getGlobalStat("gpuClauseLengthSum") == 3
     assert s.getGlobalStat("gpuReduceDbs") == 1
