@@ -542,12 +542,13 @@ constexpr uint32_t kTaskChunk = 4;
 
 template <int WPL, int LPC, int G, int MINB>
 __global__ void __launch_bounds__(kWarps * 32, MINB) check_wide_persist_kernel(const CheckArgs *__restrict__ pa,
+                                                                                const CheckArgs av,
                                                                                 uint32_t *__restrict__ work) {
     constexpr int CPW = 32 / LPC;
     constexpr int BW = WPL * LPC;
     __shared__ CheckArgs sa;
     __shared__ gss_report stage_all[kWarps][kStage];
-    if (threadIdx.x == 0) sa = *pa;
+    if (threadIdx.x == 0) sa = pa ? *pa : av;
     __syncthreads();
     const CheckArgs &a = sa;
     const int lane = threadIdx.x & 31;
@@ -656,14 +657,15 @@ __global__ void __launch_bounds__(kWarps * 32, MINB) check_wide_persist_kernel(c
 }
 
 template <int WPL, int LPC, int G>
-int launch_wide_persist_variant(const CheckArgs *d_args, uint32_t *work, cudaStream_t stream, int sm_count) {
+int launch_wide_persist_variant(const CheckArgs *d_args, const CheckArgs &h_args, uint32_t *work, cudaStream_t stream,
+                                int sm_count) {
     constexpr int MINB = default_min_blocks(WPL, G);
     int per_sm = 0;
     GSS_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, check_wide_persist_kernel<WPL, LPC, G, MINB>,
                                                                kWarps * 32, 0));
     if (per_sm < 1) per_sm = 1;
-    check_wide_persist_kernel<WPL, LPC, G, MINB><<<(unsigned) (sm_count * per_sm), kWarps * 32, 0, stream>>>(d_args,
-                                                                                                          work);
+    check_wide_persist_kernel<WPL, LPC, G, MINB><<<(unsigned) (sm_count * per_sm), kWarps * 32, 0, stream>>>(
+        d_args, h_args, work);
     GSS_CUDA_TRY(cudaGetLastError());
     return GSS_OK;
 }
@@ -762,10 +764,11 @@ int launch_check_wide_pf(const CheckArgs &a, int wpl, int occ, cudaStream_t stre
                      wpl, a.lpc, a.g);
 }
 
-int launch_check_wide_persist(const CheckArgs *d_args, int wpl, int lpc, int g, uint32_t *work, cudaStream_t stream,
-                              int sm_count) {
-#define GSS_QV(W, L, GG) \
-    if (wpl == W && lpc == L && g == GG) return launch_wide_persist_variant<W, L, GG>(d_args, work, stream, sm_count);
+int launch_check_wide_persist(const CheckArgs *d_args, const CheckArgs &h_args, int wpl, int lpc, int g, uint32_t *work,
+                              cudaStream_t stream, int sm_count) {
+#define GSS_QV(W, L, GG)                 \
+    if (wpl == W && lpc == L && g == GG) \
+        return launch_wide_persist_variant<W, L, GG>(d_args, h_args, work, stream, sm_count);
     GSS_QV(4, 8, 1) GSS_QV(4, 8, 2) GSS_QV(4, 8, 4)
     GSS_QV(4, 4, 2) GSS_QV(4, 2, 2)
     GSS_QV(2, 16, 2) GSS_QV(2, 8, 2)

@@ -169,10 +169,12 @@ int launch_check_wide(const CheckArgs &a, int wpl, int occ, cudaStream_t stream,
 // Pipelined wide kernel (occ: 4 blocks per SM register cap).
 int launch_check_wide_pf(const CheckArgs &a, int wpl, int occ, cudaStream_t stream, int sm_count);
 bool valid_wide_pf_variant(int wpl, int lpc, int g);
-// Persistent wide kernel: arguments read from device memory (d_args), tasks
-// from the device counter `work` (zero it before each launch).
-int launch_check_wide_persist(const CheckArgs *d_args, int wpl, int lpc, int g, uint32_t *work, cudaStream_t stream,
-                              int sm_count);
+// Persistent wide kernel: arguments read from device memory (d_args, so that
+// a captured graph serves every pass) or, when d_args is NULL, passed by
+// value (h_args); tasks from the device counter `work` (zero it before each
+// launch).
+int launch_check_wide_persist(const CheckArgs *d_args, const CheckArgs &h_args, int wpl, int lpc, int g, uint32_t *work,
+                              cudaStream_t stream, int sm_count);
 bool valid_wide_persist_variant(int wpl, int lpc, int g);
 bool valid_wide_variant(int wpl, int lpc, int g, int occ);
 bool valid_tiled_variant(int lpc, int k);

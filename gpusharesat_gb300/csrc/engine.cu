@@ -858,15 +858,24 @@ int launch_pass_into(gss_engine *eng, const void *state, DevBuf &reports, DevBuf
     const bool wide = eng->state_kind == GSS_KERNEL_WIDE4 || eng->state_kind == GSS_KERNEL_WIDE2;
     const bool ordered = order_active(eng);
     const bool bucketed = !eng->plan_layout.empty();
-    if (ordered && (eng->state_kind == GSS_KERNEL_TILED || (eng->flags & GSS_VARIANT_PERSISTENT) || bucketed))
-        return set_error(GSS_ERR_STATE, "the learned scan order runs the direct and wide kernels (not the tiled, "
-                         "persistent or bucketed ones)");
+    // The automatic variant runs the persistent form of the wide kernel: tasks
+    // from a work counter keep the warps on neighbouring clause groups (the
+    // database order's L2 locality holds) and balance uneven clause lengths;
+    // measured 0.91 ms against 1.13 ms for the grid-stride form on the
+    // at-scale workload.
+    const bool persistent =
+        wide && ((eng->flags & GSS_VARIANT_PERSISTENT) ||
+                 (eng->kind == GSS_KERNEL_AUTO &&
+                  valid_wide_persist_variant(words_per_lane(eng->state_kind), eng->state_lpc, eng->state_g)));
+    if (ordered && (eng->state_kind == GSS_KERNEL_TILED || bucketed))
+        return set_error(GSS_ERR_STATE, "the learned scan order runs the direct, wide and persistent kernels (not the "
+                         "tiled or bucketed ones)");
     if (bucketed && eng->n_words > 0 && eng->state_bw != 32)
         return set_error(GSS_ERR_STATE, "the length plan needs a state laid out in 32-word blocks (%d here)",
                          eng->state_bw);
     if (ordered && (&reports != &eng->reports || &counts != &eng->counts))
         return set_error(GSS_ERR_STATE, "the learned scan order runs through gss_check_launch");
-    if (bucketed || (wide && (eng->flags & GSS_VARIANT_PERSISTENT))) {
+    if (bucketed || (persistent && eng->use_graph && !ordered)) {
         // arguments through device memory, so the same graph serves every pass
         if (bucketed) GSS_TRY(build_plan(eng));
         GSS_TRY(eng->d_args.reserve(sizeof(CheckArgs)));
@@ -884,7 +893,7 @@ int launch_pass_into(gss_engine *eng, const void *state, DevBuf &reports, DevBuf
                                                       (const BucketPlan *) eng->d_plan.ptr, (uint32_t *) eng->work.ptr,
                                                       eng->stream, eng->sm_count));
                 } else {
-                    GSS_TRY(launch_check_wide_persist((const CheckArgs *) eng->d_args.ptr,
+                    GSS_TRY(launch_check_wide_persist((const CheckArgs *) eng->d_args.ptr, a,
                                                       words_per_lane(eng->state_kind), eng->state_lpc, eng->state_g,
                                                       (uint32_t *) eng->work.ptr, eng->stream, eng->sm_count));
                 }
@@ -930,8 +939,16 @@ int launch_pass_into(gss_engine *eng, const void *state, DevBuf &reports, DevBuf
     GSS_CUDA_TRY(cudaMemsetAsync(a.counts, 0, sizeof(uint32_t) * a.n_parts, eng->stream));
     GSS_CUDA_TRY(cudaMemsetAsync(a.err, 0, sizeof(uint32_t), eng->stream));
     if (ev0) GSS_CUDA_TRY(cudaEventRecord(ev0, eng->stream));
+    if (persistent) GSS_TRY(eng->work.reserve(sizeof(uint32_t)));
     auto launch = [&](const CheckArgs &args) -> int {
         if (eng->state_kind == GSS_KERNEL_TILED) return launch_check_tiled(args, eng->stream, eng->sm_count);
+        if (persistent) {
+            // arguments by value; the work counter restarts for each launch
+            GSS_CUDA_TRY(cudaMemsetAsync(eng->work.ptr, 0, sizeof(uint32_t), eng->stream));
+            if (args.n_clauses == 0 || args.n_blocks == 0 || scan_count(args) == 0) return GSS_OK;
+            return launch_check_wide_persist(nullptr, args, words_per_lane(eng->state_kind), eng->state_lpc,
+                                             eng->state_g, (uint32_t *) eng->work.ptr, eng->stream, eng->sm_count);
+        }
         const int occ = (eng->flags & GSS_VARIANT_OCCUPANCY) ? 1 : 0;
         if (wide && (eng->flags & GSS_VARIANT_PIPELINED))
             return launch_check_wide_pf(args, words_per_lane(eng->state_kind), occ, eng->stream, eng->sm_count);

@@ -100,7 +100,8 @@ int gss_engine_set_timing(gss_engine *eng, int on);
 int gss_engine_kernel_time(gss_engine *eng, double *total_ms, int64_t *n_launches);
 
 /* Check-kernel kinds. */
-#define GSS_KERNEL_AUTO -1   /* default: picked from the word count at gss_state_set */
+#define GSS_KERNEL_AUTO -1   /* default: picked from the word count at gss_state_set (8 words or more: the
+                                wide kernel in its persistent form, 4 words per lane) */
 #define GSS_KERNEL_DIRECT 0  /* a lane group per clause, one 32-slot word per lane */
 #define GSS_KERNEL_TILED 1   /* clause tiles staged in shared memory by bulk copy, K clause slots */
 #define GSS_KERNEL_WIDE4 2   /* a lane group per clause, four words per lane (256-bit loads) */
@@ -109,8 +110,9 @@ int gss_engine_kernel_time(gss_engine *eng, double *total_ms, int64_t *n_launche
 #define GSS_VARIANT_L2_HINT 1    /* L2 evict-last policy on state loads (direct, tiled) */
 #define GSS_VARIANT_OCCUPANCY 2  /* compile-time register cap: 8 blocks per SM (wide), 4 (pipelined wide) */
 #define GSS_VARIANT_PIPELINED 4  /* wide kinds: next clause's offsets and literals loaded ahead */
-#define GSS_VARIANT_PERSISTENT 8 /* wide kinds: one CTA set for the whole pass, tasks from a work counter,
-                                    arguments from device memory (what gss_engine_set_graph replays) */
+#define GSS_VARIANT_PERSISTENT 8 /* wide kinds: one CTA set for the whole pass, tasks from a work counter;
+                                    arguments by value, or from device memory when gss_engine_set_graph
+                                    replays the pass */
 /* Lane layouts of the bucketed kernel (gss_engine_set_length_plan): words
  * per lane x lanes per clause (always one 32-word state row per slot block),
  * and loads in flight per lane. GSS_LAYOUT_SKIP leaves a length class out of

@@ -129,6 +129,34 @@ def test_ordered_pass_reports_equal_plain(lib):
     eng.close()
 
 
+@pytest.mark.parametrize("variant", [None, (2, 8, 2, 0), (2, 8, 2, 8)])
+def test_ordered_wide_and_persistent_passes_equal_oracle(lib, variant):
+    """The learned order over the wide kernel, grid-stride or persistent (the
+    automatic choice at 32 words): head plus tail is the oracle's set."""
+    import gpusharesat_gb300 as g
+    import oracle
+    from gpusharesat_gb300 import workloads as W
+    wl = W.make_scale(seed=12, n_vars=2 ** 14, n_clauses=30000, n_solvers=32)
+    eng = g.Engine(0)
+    try:
+        if variant:
+            eng.set_variant(*variant)
+        eng.set_db(wl.lits, wl.offsets)
+        eng.set_state(wl.state, wl.start, wl.solver_of_word)
+        eng.set_capacity(1 << 21)
+        eng.order_enable(head_fraction=0.25, retrain_interval=0)
+        ref = oracle.check(wl.lits, wl.offsets, wl.state, wl.start, n_threads=8)
+        want = set(zip(ref["clause"].tolist(), ref["word"].tolist(), ref["mask"].tolist()))
+        for _ in range(3):
+            eng.launch()
+            head = eng.wait_head()
+            got = np.concatenate([head, eng.copy_tail()])
+            assert len(got) == len(ref)
+            assert set(zip(got["clause"].tolist(), got["word"].tolist(), got["mask"].tolist())) == want
+    finally:
+        eng.close()
+
+
 def test_order_features_follow_the_report_history(lib):
     eng, wl = _small_engine(head_fraction=0.25, retrain_interval=0)
     n = wl.n_clauses
