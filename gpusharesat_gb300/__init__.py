@@ -41,6 +41,7 @@ LAYOUT_1x32_G2 = 5
 LAYOUTS = (LAYOUT_4x8_G1, LAYOUT_4x8_G2, LAYOUT_2x16_G1, LAYOUT_2x16_G2, LAYOUT_1x32_G1, LAYOUT_1x32_G2)
 
 REPORT_DTYPE = np.dtype([("clause", "<u4"), ("word", "<u4"), ("mask", "<u4"), ("solver", "<u4")])
+PACKED_REPORT_DTYPE = np.dtype([("clause", "<u4"), ("word", "<u4"), ("mask", "<u4")])
 
 _lib = None
 
@@ -102,6 +103,7 @@ def load():
     _sig(lib, "gss_check_copy_reports", c_int, vp, vp, c_i64, vp)
     _sig(lib, "gss_check_pass_host", c_int, vp, vp, c_i64, c_int, vp, vp, vp, c_i64, vp)
     _sig(lib, "gss_check_passes_host", c_int, vp, c_int, vp, c_i64, c_int, vp, vp, vp, vp, vp)
+    _sig(lib, "gss_check_passes_host_packed", c_int, vp, c_int, vp, c_i64, c_int, vp, vp, vp, vp, vp)
     _sig(lib, "gss_db_positions", c_int, vp, vp, c_i64, vp)
     _sig(lib, "gss_engine_set_length_plan", c_int, vp, c_int, vp, vp)
     _sig(lib, "gss_order_params_default", None, vp)
@@ -487,9 +489,10 @@ def bench_plant(lits_ptr, offsets_ptr, n_clauses, rate_ptr, state_ptr, base_ptr,
                                _vp(stream) if stream else None))
 
 
-def passes_host(engine, states, start, solver_of_word=None, caps=None):
-    """Pipelined passes through host buffers (gss_check_passes_host); returns
-    one report array per state."""
+def passes_host(engine, states, start, solver_of_word=None, caps=None, packed=False):
+    """Pipelined passes through host buffers (gss_check_passes_host, or
+    gss_check_passes_host_packed for 12-byte records); returns one report
+    array per state."""
     lib = engine.lib
     n = len(states)
     states = [np.ascontiguousarray(s, dtype=np.uint32) for s in states]
@@ -497,13 +500,14 @@ def passes_host(engine, states, start, solver_of_word=None, caps=None):
     sow = None if solver_of_word is None else np.ascontiguousarray(solver_of_word, dtype=np.int32)
     caps = caps or [1 << 20] * n
     while True:
-        outs = [np.zeros(max(int(c), 1), dtype=REPORT_DTYPE) for c in caps]
+        outs = [np.zeros(max(int(c), 1), dtype=PACKED_REPORT_DTYPE if packed else REPORT_DTYPE) for c in caps]
         sp = (ctypes.c_void_p * n)(*[s.ctypes.data for s in states])
         op = (ctypes.c_void_p * n)(*[o.ctypes.data for o in outs])
         cp = np.ascontiguousarray(caps, dtype=np.int64)
         nr = np.zeros(n, dtype=np.int64)
-        rc = lib.gss_check_passes_host(engine.h, n, sp, states[0].shape[0], states[0].shape[1], _ptr(start), _ptr(sow),
-                                       op, _ptr(cp), _ptr(nr))
+        fn = lib.gss_check_passes_host_packed if packed else lib.gss_check_passes_host
+        rc = fn(engine.h, n, sp, states[0].shape[0], states[0].shape[1], _ptr(start), _ptr(sow), op, _ptr(cp),
+                _ptr(nr))
         if rc == GSS_ERR_OVERFLOW:
             caps = [max(int(c), int(x)) + 1024 for c, x in zip(caps, nr)]
             continue

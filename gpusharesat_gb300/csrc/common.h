@@ -25,6 +25,15 @@ constexpr int kBufLits = kTileLits + 8;
 // stay inside the buffer.
 constexpr int kClausePad = 8;
 
+// Database order by variable ranges of 2^shift variables: the key of a
+// clause is (its most frequent range, its second range, its length);
+// `reordered` (optional, len entries) receives its literals with those of
+// the most frequent range first, then the second range's, and so on.
+uint64_t range_order_key(const int32_t *lits, int64_t len, int shift, int32_t *reordered);
+// The range shift for a database whose largest variable is max_var
+// (range_log2: -1 automatic = 17, 0 = no ranges); 0 when one range would do.
+int range_shift_for(int64_t max_var, int range_log2);
+
 // Sets the calling thread's error message and returns `code`.
 int set_error(int code, const char *fmt, ...);
 
@@ -157,6 +166,10 @@ struct GatherArgs {
     uint32_t *new_ids;     // room for n_new
 };
 int gather_clauses(const GatherArgs &a, cudaStream_t stream, int sm_count);
+// Packs report partitions (n_parts x cap records, counts[p] valid in
+// partition p, device) into contiguous 12-byte {clause, word, mask} records.
+int launch_pack_reports(const gss_report *parts, const uint32_t *counts, uint32_t n_parts, uint32_t cap,
+                        uint32_t *packed, cudaStream_t stream, int sm_count);
 // Synchronizes `stream`; returns the live clause and literal counts.
 int compact_by_id(const CompactArgs &a, cudaStream_t stream, int sm_count, uint32_t *n_out, int64_t *lits_out);
 

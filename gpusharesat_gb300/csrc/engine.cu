@@ -103,6 +103,45 @@ void PinnedBuf::release() {
     bytes = 0;
 }
 
+// Variable-range order key of one clause (see range_order) and, into
+// `reordered` when given, its literals with the most frequent range first.
+uint64_t range_order_key(const int32_t *lits, int64_t len, int shift, int32_t *reordered) {
+    thread_local std::vector<std::pair<int32_t, int32_t>> cnt;  // (range, count)
+    cnt.clear();
+    for (int64_t i = 0; i < len; i++) {
+        const int32_t r = (int32_t) ((uint32_t) lits[i] >> 1 >> shift);
+        bool found = false;
+        for (auto &p : cnt)
+            if (p.first == r) {
+                p.second++;
+                found = true;
+                break;
+            }
+        if (!found) cnt.push_back({r, 1});
+    }
+    std::sort(cnt.begin(), cnt.end(), [](const std::pair<int32_t, int32_t> &x, const std::pair<int32_t, int32_t> &y) {
+        return x.second != y.second ? x.second > y.second : x.first < y.first;
+    });
+    if (reordered) {
+        int64_t o = 0;
+        for (const auto &p : cnt)
+            for (int64_t i = 0; i < len; i++)
+                if ((int32_t) ((uint32_t) lits[i] >> 1 >> shift) == p.first) reordered[o++] = lits[i];
+    }
+    if (cnt.empty()) return (uint64_t) len;
+    const uint64_t home = (uint64_t) cnt[0].first;
+    const uint64_t second = cnt.size() > 1 ? (uint64_t) cnt[1].first : home;
+    // 20 bits per range index (ranges of 2^11 variables or more), 13 for the length
+    return (home << 33) | (second << 13) | (uint64_t) len;
+}
+
+int range_shift_for(int64_t max_var, int range_log2) {
+    const int shift = range_log2 < 0 ? 17 : range_log2;
+    if (shift == 0 || max_var < 0 || (max_var >> shift) == 0) return 0;
+    return shift;
+}
+
+
 }  // namespace gss
 
 using namespace gss;
@@ -340,34 +379,11 @@ int upload_all(gss_engine *eng) {
 void range_order(const int32_t *lits, const int64_t *offsets, int64_t n, int shift, std::vector<uint32_t> &order,
                  std::vector<int32_t> &relits) {
     std::vector<std::pair<uint64_t, uint32_t>> keys((size_t) n);
-    std::vector<std::pair<int32_t, int32_t>> cnt;  // (range, count) of one clause
     const int64_t base = n > 0 ? offsets[0] : 0;
     relits.resize((size_t) (n > 0 ? offsets[n] - base : 0));
     for (int64_t c = 0; c < n; c++) {
         const int64_t b = offsets[c], e = offsets[c + 1];
-        cnt.clear();
-        for (int64_t i = b; i < e; i++) {
-            const int32_t r = (int32_t) ((uint32_t) lits[i] >> 1 >> shift);
-            bool found = false;
-            for (auto &p : cnt)
-                if (p.first == r) {
-                    p.second++;
-                    found = true;
-                    break;
-                }
-            if (!found) cnt.push_back({r, 1});
-        }
-        std::sort(cnt.begin(), cnt.end(), [](const std::pair<int32_t, int32_t> &x, const std::pair<int32_t, int32_t> &y) {
-            return x.second != y.second ? x.second > y.second : x.first < y.first;
-        });
-        int64_t o = b - base;
-        for (const auto &p : cnt)
-            for (int64_t i = b; i < e; i++)
-                if ((int32_t) ((uint32_t) lits[i] >> 1 >> shift) == p.first) relits[(size_t) o++] = lits[i];
-        const uint64_t home = (uint64_t) cnt[0].first;
-        const uint64_t second = cnt.size() > 1 ? (uint64_t) cnt[1].first : home;
-        // 20 bits per range index (ranges of 2^11 variables or more), 13 for the length
-        keys[c] = {(home << 33) | (second << 13) | (uint64_t) (e - b), (uint32_t) c};
+        keys[c] = {range_order_key(lits + b, e - b, shift, relits.data() + (b - base)), (uint32_t) c};
     }
     std::sort(keys.begin(), keys.end());
     order.resize((size_t) n);
@@ -377,11 +393,7 @@ void range_order(const int32_t *lits, const int64_t *offsets, int64_t n, int shi
 // log2 of the variables per range for a database whose largest variable is
 // max_var: ranges of 2^17 variables (32 MB of state rows at 32 words per
 // block) by default; 0 (no ranges) when there would be a single range.
-int effective_range_shift(const gss_engine *eng, int64_t max_var) {
-    int shift = eng->range_log2 < 0 ? 17 : eng->range_log2;
-    if (shift == 0 || max_var < 0 || (max_var >> shift) == 0) return 0;
-    return shift;
-}
+int effective_range_shift(const gss_engine *eng, int64_t max_var) { return range_shift_for(max_var, eng->range_log2); }
 
 // Adds a batch to the host mirror in length order (or variable-range order,
 // see range_order); returns the first index.
@@ -1051,9 +1063,15 @@ int gss_check_pass_host(gss_engine *eng, const uint32_t *state, int64_t n_vars, 
     return set_error(GSS_ERR_OVERFLOW, "report queues kept overflowing");
 }
 
-int gss_check_passes_host(gss_engine *eng, int n_passes, const uint32_t *const *states, int64_t n_vars,
-                          int n_words, const uint32_t *start, const int32_t *solver_of_word, gss_report *const *outs,
-                          const int64_t *caps, int64_t *n_reports) {
+}  // extern "C"
+
+namespace {
+
+// Passes through host buffers; outs[i] receives gss_report records, or
+// 12-byte {clause, word, mask} records packed on the device when `packed`.
+int passes_host(gss_engine *eng, int n_passes, const uint32_t *const *states, int64_t n_vars, int n_words,
+                const uint32_t *start, const int32_t *solver_of_word, void *const *outs, const int64_t *caps,
+                int64_t *n_reports, bool packed) {
     // Passes i = 0..n-1 over three streams: the state of pass i+1 goes
     // host->device (h2d stream) and the reports of pass i-1 come back (d2h
     // stream) while pass i runs (engine stream). Double buffers: state b and
@@ -1082,6 +1100,18 @@ int gss_check_passes_host(gss_engine *eng, int n_passes, const uint32_t *const *
     }
     GSS_TRY(eng->reports2.reserve((size_t) eng->cap_per_part * eng->n_parts * sizeof(gss_report)));
     GSS_TRY(eng->counts2.reserve(sizeof(uint32_t) * eng->n_parts));
+    auto reserve_packed = [&]() -> int {
+        for (int b = 0; b < 2 && packed; b++)
+            GSS_TRY(eng->packed[b].reserve((size_t) eng->cap_per_part * eng->n_parts * 3 * sizeof(uint32_t)));
+        return GSS_OK;
+    };
+    GSS_TRY(reserve_packed());
+    // packs pass b's reports (after its check, on the engine stream)
+    auto pack = [&](int b, const DevBuf &rep, const DevBuf &cnt) -> int {
+        if (!packed) return GSS_OK;
+        return launch_pack_reports((const gss_report *) rep.ptr, (const uint32_t *) cnt.ptr, eng->n_parts,
+                                   eng->cap_per_part, (uint32_t *) eng->packed[b].ptr, eng->stream, eng->sm_count);
+    };
     GSS_TRY(eng->h_counts2.reserve(sizeof(uint32_t) * (eng->n_parts + 1)));
     DevBuf *state_buf[2] = {&eng->state, &eng->state2};
     DevBuf *raw_buf[2] = {&eng->state_raw, &eng->state_raw2};
@@ -1113,12 +1143,15 @@ int gss_check_passes_host(gss_engine *eng, int n_passes, const uint32_t *const *
             eng->requested_cap = std::max<int64_t>(eng->requested_cap, total * 2 + eng->n_parts * 1024);
             GSS_TRY(ensure_queues(eng));
             GSS_TRY(eng->reports2.reserve((size_t) eng->cap_per_part * eng->n_parts * sizeof(gss_report)));
+            GSS_TRY(reserve_packed());
             GSS_TRY(launch_pass_into(eng, state_buf[b]->ptr, *rep_buf[b], *cnt_buf[b], *hcnt_buf[b]));
+            GSS_TRY(pack(b, *rep_buf[b], *cnt_buf[b]));
             eng->launches++;
             GSS_CUDA_TRY(cudaEventRecord(eng->ev_kernel[b], eng->stream));
             if (j + 1 < launched) {
                 const int nb = b ^ 1;
                 GSS_TRY(launch_pass_into(eng, state_buf[nb]->ptr, *rep_buf[nb], *cnt_buf[nb], *hcnt_buf[nb]));
+                GSS_TRY(pack(nb, *rep_buf[nb], *cnt_buf[nb]));
                 eng->launches++;
                 GSS_CUDA_TRY(cudaEventRecord(eng->ev_kernel[nb], eng->stream));
             }
@@ -1130,12 +1163,19 @@ int gss_check_passes_host(gss_engine *eng, int n_passes, const uint32_t *const *
         if (total > caps[j])
             return set_error(GSS_ERR_OVERFLOW, "output %d holds %lld records, pass has %lld", j, (long long) caps[j],
                              (long long) total);
-        int64_t pos = 0;
-        for (uint32_t p = 0; p < eng->n_parts; p++) {
-            if (!hc[p]) continue;
-            GSS_CUDA_TRY(cudaMemcpyAsync(outs[j] + pos, (gss_report *) rep_buf[b]->ptr + (size_t) p * eng->cap_per_part,
-                                         (size_t) hc[p] * sizeof(gss_report), cudaMemcpyDeviceToHost, eng->d2h));
-            pos += hc[p];
+        if (packed) {
+            if (total)
+                GSS_CUDA_TRY(cudaMemcpyAsync(outs[j], eng->packed[b].ptr, (size_t) total * 3 * sizeof(uint32_t),
+                                             cudaMemcpyDeviceToHost, eng->d2h));
+        } else {
+            int64_t pos = 0;
+            for (uint32_t p = 0; p < eng->n_parts; p++) {
+                if (!hc[p]) continue;
+                GSS_CUDA_TRY(cudaMemcpyAsync((gss_report *) outs[j] + pos,
+                                             (gss_report *) rep_buf[b]->ptr + (size_t) p * eng->cap_per_part,
+                                             (size_t) hc[p] * sizeof(gss_report), cudaMemcpyDeviceToHost, eng->d2h));
+                pos += hc[p];
+            }
         }
         GSS_CUDA_TRY(cudaEventRecord(eng->ev_d2h[b], eng->d2h));
         return GSS_OK;
@@ -1160,6 +1200,7 @@ int gss_check_passes_host(gss_engine *eng, int n_passes, const uint32_t *const *
         // report set b is free once pass i-2's reports are back
         if (i >= 2) GSS_CUDA_TRY(cudaStreamWaitEvent(eng->stream, eng->ev_d2h[b], 0));
         GSS_TRY(launch_pass_into(eng, state_buf[b]->ptr, *rep_buf[b], *cnt_buf[b], *hcnt_buf[b]));
+        GSS_TRY(pack(b, *rep_buf[b], *cnt_buf[b]));
         eng->launches++;
         launched = i + 1;
         GSS_CUDA_TRY(cudaEventRecord(eng->ev_kernel[b], eng->stream));
@@ -1175,6 +1216,24 @@ int gss_check_passes_host(gss_engine *eng, int n_passes, const uint32_t *const *
     if (rc != GSS_OK) cudaDeviceSynchronize();
     eng->pass_pending = false;
     return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gss_check_passes_host(gss_engine *eng, int n_passes, const uint32_t *const *states, int64_t n_vars,
+                          int n_words, const uint32_t *start, const int32_t *solver_of_word, gss_report *const *outs,
+                          const int64_t *caps, int64_t *n_reports) {
+    return passes_host(eng, n_passes, states, n_vars, n_words, start, solver_of_word, (void *const *) outs, caps,
+                       n_reports, false);
+}
+
+int gss_check_passes_host_packed(gss_engine *eng, int n_passes, const uint32_t *const *states, int64_t n_vars,
+                                 int n_words, const uint32_t *start, const int32_t *solver_of_word,
+                                 gss_report_packed *const *outs, const int64_t *caps, int64_t *n_reports) {
+    return passes_host(eng, n_passes, states, n_vars, n_words, start, solver_of_word, (void *const *) outs, caps,
+                       n_reports, true);
 }
 
 }  // extern "C"

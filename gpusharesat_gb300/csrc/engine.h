@@ -73,6 +73,7 @@ struct gss_engine {
     // pipelined passes through host buffers (gss_check_passes_host): second
     // state and report buffers, copy streams and events
     DevBuf state2, state_raw2, reports2, counts2;
+    DevBuf packed[2];  // 12-byte records of gss_check_passes_host_packed
     PinnedBuf h_counts2;
     cudaStream_t h2d = nullptr, d2h = nullptr;
     cudaEvent_t ev_h2d[2] = {nullptr, nullptr}, ev_kernel[2] = {nullptr, nullptr}, ev_d2h[2] = {nullptr, nullptr};

@@ -31,6 +31,7 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <condition_variable>
 #include <mutex>
 #include <thread>
 #include <vector>
@@ -181,6 +182,30 @@ int gss_serving_run(const gss_serving_params *p, gss_serving_result *res) {
     std::atomic<bool> stop{false};
     std::atomic<int> gpu_error{0};
     std::atomic<int64_t> streamed{0}, passes{0};
+    // Solver threads sleep until the next pass ends or their next arrival,
+    // instead of polling: 64 polling threads on a 16-core host would take the
+    // CPU from the thread that runs the passes.
+    std::mutex pass_lock;
+    std::condition_variable pass_done;
+    int64_t pass_seq = 0;
+    auto notify_pass = [&]() {
+        {
+            std::lock_guard<std::mutex> g(pass_lock);
+            pass_seq++;
+        }
+        pass_done.notify_all();
+    };
+    // waits for a pass after `seen`, or until `deadline_s` (seconds since t0)
+    auto wait_pass = [&](int64_t seen, double deadline_s) {
+        std::unique_lock<std::mutex> g(pass_lock);
+        const auto until = t0 + std::chrono::duration_cast<Clock::duration>(std::chrono::duration<double>(deadline_s));
+        pass_done.wait_until(g, until, [&]() { return pass_seq != seen || stop.load(); });
+        return pass_seq;
+    };
+    auto pass_now = [&]() {
+        std::lock_guard<std::mutex> g(pass_lock);
+        return pass_seq;
+    };
     int64_t tested_at_measure = -1;
     double time_at_measure = 0;
     std::mutex measure_lock;
@@ -233,9 +258,11 @@ int gss_serving_run(const gss_serving_params *p, gss_serving_result *res) {
             if (gss_sharer_gpu_run(sh) != GSS_OK) {
                 gpu_error = 1;
                 stop = true;
+                notify_pass();
                 break;
             }
             passes++;
+            notify_pass();
         }
     });
 
@@ -296,18 +323,20 @@ int gss_serving_run(const gss_serving_params *p, gss_serving_result *res) {
                         }
                     }
                     if (!del.empty()) gss_sharer_unset_solver_values(sh, s, del.data(), (int) del.size());
+                    // a full ring frees at the next pass's cut: wait for it
+                    int64_t seen = pass_now();
                     while (!gss_sharer_try_set_solver_values(sh, s, add.data(), (int) add.size())) {
                         sv.retries++;
                         poll();
                         if (stop.load()) break;
-                        std::this_thread::sleep_for(std::chrono::microseconds(20));
+                        seen = wait_pass(seen, now_s(t0) + 0.002);
                     }
                     int64_t id;
                     while ((id = gss_sharer_try_send_assignment(sh, s)) < 0) {
                         sv.retries++;
                         poll();
                         if (stop.load()) break;
-                        std::this_thread::sleep_for(std::chrono::microseconds(20));
+                        seen = wait_pass(seen, now_s(t0) + 0.002);
                     }
                     if (id >= 0) {
                         if ((int64_t) sv.arrival.size() <= id) sv.arrival.resize(id + 1);
@@ -315,8 +344,11 @@ int gss_serving_run(const gss_serving_params *p, gss_serving_result *res) {
                     }
                     pending_batch--;
                 } else {
+                    // deliveries come with passes: sleep until the next one
+                    // ends or the next batch arrives
+                    const int64_t seen = pass_now();
                     poll();
-                    std::this_thread::sleep_for(std::chrono::microseconds(20));
+                    wait_pass(seen, std::min(next_arrival, t_end));
                 }
             }
         });
@@ -325,6 +357,7 @@ int gss_serving_run(const gss_serving_params *p, gss_serving_result *res) {
     const double t_stop = now_s(t0);
     const int64_t tested_end = gss_sharer_global_stat(sh, 6);
     stop = true;
+    notify_pass();
     for (auto &t : threads) t.join();
     gpu.join();
 

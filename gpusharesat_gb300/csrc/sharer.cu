@@ -291,6 +291,11 @@ int Sharer::set_variant(int kind, int lpc, int depth, int flags) {
         !valid_wide_variant(kind == GSS_KERNEL_WIDE4 ? 4 : 2, lpc ? lpc : (kind == GSS_KERNEL_WIDE4 ? 8 : 16), depth,
                             (flags & GSS_VARIANT_OCCUPANCY) ? 1 : 0))
         return set_error(GSS_ERR_INVALID, "no wide kernel variant for %d lanes per clause, depth %d", lpc, depth);
+    if ((kind == GSS_KERNEL_WIDE4 || kind == GSS_KERNEL_WIDE2) && (flags & GSS_VARIANT_PERSISTENT) &&
+        !valid_wide_persist_variant(kind == GSS_KERNEL_WIDE4 ? 4 : 2, lpc ? lpc : (kind == GSS_KERNEL_WIDE4 ? 8 : 16),
+                                    depth))
+        return set_error(GSS_ERR_INVALID, "no persistent wide kernel variant for %d lanes per clause, depth %d", lpc,
+                         depth);
     kind_ = kind;
     lpc_req_ = lpc;
     depth_req_ = depth;
@@ -723,8 +728,18 @@ int Sharer::append_clauses(std::vector<int64_t> &ids, std::vector<int32_t> &lits
         stats_[kGpuClauses]++;
         stats_[kGpuClauseLengthSum] += lens[i];
     }
-    // device order of this batch: by length (warps then check equal lengths)
-    std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return lens[a] < lens[b]; });
+    // Device order of this batch: by length (warps then check equal
+    // lengths), and with a large variable count by (variable range, second
+    // range, length) with each clause's device literals grouped by range, as
+    // the engine's database order (range_order_key). The host arena keeps
+    // the literals as the solver gave them, for delivery.
+    const int shift = range_shift_for(max_var_, -1);
+    std::vector<uint64_t> key(ids.size());
+    std::vector<int32_t> relits(shift ? lits.size() : 0);
+    for (size_t i = 0; i < ids.size(); i++)
+        key[i] = shift ? range_order_key(&lits[starts[i]], lens[i], shift, &relits[starts[i]]) : lens[i];
+    std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return key[a] < key[b]; });
+    const std::vector<int32_t> &dev_src = shift ? relits : lits;
     std::vector<ClauseMeta> sorted(ids.size());
     // the new clauses go after the device's last clause
     const int64_t base_off = dev_lits_;
@@ -739,7 +754,7 @@ int Sharer::append_clauses(std::vector<int64_t> &ids, std::vector<int32_t> &lits
         ClauseMeta m = meta_[first + i];
         m.lit_off = (uint32_t) (h_lits_.size());
         h_lits_.insert(h_lits_.end(), lits.begin() + starts[i], lits.begin() + starts[i] + lens[i]);
-        new_lits.insert(new_lits.end(), lits.begin() + starts[i], lits.begin() + starts[i] + lens[i]);
+        new_lits.insert(new_lits.end(), dev_src.begin() + starts[i], dev_src.begin() + starts[i] + lens[i]);
         sorted[k] = m;
         end_off += lens[i];
         new_offsets.push_back(end_off);
@@ -856,9 +871,17 @@ int Sharer::run_check(Pass &p) {
     GSS_CUDA_TRY(cudaMemsetAsync(a.counts, 0, sizeof(uint32_t) * n_parts_, stream_));
     GSS_CUDA_TRY(cudaMemsetAsync(a.err, 0, sizeof(uint32_t), stream_));
     if (p.active_words > 0 && p.n_clauses > 0) {
-        if (eff_kind_ == GSS_KERNEL_WIDE4 || eff_kind_ == GSS_KERNEL_WIDE2) {
-            GSS_TRY(launch_check_wide(a, eff_kind_ == GSS_KERNEL_WIDE4 ? 4 : 2,
-                                      (flags_ & GSS_VARIANT_OCCUPANCY) ? 1 : 0, stream_, sm_count_));
+        const int wpl = eff_kind_ == GSS_KERNEL_WIDE4 ? 4 : 2;
+        const bool wide = eff_kind_ == GSS_KERNEL_WIDE4 || eff_kind_ == GSS_KERNEL_WIDE2;
+        if (wide && ((flags_ & GSS_VARIANT_PERSISTENT) ||
+                     (kind_ == GSS_KERNEL_AUTO && valid_wide_persist_variant(wpl, eff_lpc_, eff_depth_)))) {
+            // the persistent form, as the engine's automatic variant
+            GSS_TRY(d_work_.reserve(sizeof(uint32_t)));
+            GSS_CUDA_TRY(cudaMemsetAsync(d_work_.ptr, 0, sizeof(uint32_t), stream_));
+            GSS_TRY(launch_check_wide_persist(nullptr, a, wpl, eff_lpc_, eff_depth_, (uint32_t *) d_work_.ptr, stream_,
+                                              sm_count_));
+        } else if (wide) {
+            GSS_TRY(launch_check_wide(a, wpl, (flags_ & GSS_VARIANT_OCCUPANCY) ? 1 : 0, stream_, sm_count_));
         } else {
             GSS_TRY(launch_check(a, stream_, sm_count_));
         }
@@ -1186,9 +1209,15 @@ int Sharer::reduce_now(bool on_device) {
         }
     }
     act_->compact(keep);
+    // the kept clauses in the device order of appended batches (length, or
+    // variable range, second range, length)
+    const int shift = range_shift_for(max_var_, -1);
+    std::vector<uint64_t> key(kept.size());
+    for (size_t k = 0; k < kept.size(); k++)
+        key[k] = shift ? range_order_key(&h_lits_[kept[k].lit_off], kept[k].len, shift, nullptr) : kept[k].len;
     std::vector<uint32_t> order(kept.size());
     for (uint32_t i = 0; i < order.size(); i++) order[i] = i;
-    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return kept[a].len < kept[b].len; });
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return key[a] < key[b]; });
     const uint32_t n = (uint32_t) kept.size();
     meta_.resize(n);
     std::vector<uint32_t> src(std::max<uint32_t>(n, 1));

@@ -272,7 +272,7 @@ private:
     int eff_kind_ = GSS_KERNEL_DIRECT, eff_lpc_ = 1, eff_depth_ = 2, bw_ = 1, n_blocks_ = 0;
 
     // reports: two passes, alternating (the one launched last is pass_[cur_])
-    DevBuf d_err_;
+    DevBuf d_err_, d_work_;  // kernel error flag, persistent kernel's task counter
     uint32_t n_parts_ = 16;
     uint32_t report_cap_ = 0;  // records per partition that earlier passes needed
     Pass pass_[2];

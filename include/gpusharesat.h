@@ -231,6 +231,18 @@ int gss_check_pass_host(gss_engine *eng, const uint32_t *state, int64_t n_vars, 
 int gss_check_passes_host(gss_engine *eng, int n_passes, const uint32_t *const *states, int64_t n_vars,
                           int n_words, const uint32_t *start, const int32_t *solver_of_word,
                           gss_report *const *outs, const int64_t *caps, int64_t *n_reports);
+/* The same passes with the reports packed on the device into 12-byte
+ * records {clause, word, mask} (the solver of a word is the caller's
+ * solver_of_word[word]): a quarter less to copy back over the host link,
+ * which bounds a pass through host buffers. No counterpart in the reference. */
+typedef struct gss_report_packed {
+    uint32_t clause;
+    uint32_t word;
+    uint32_t mask;
+} gss_report_packed;
+int gss_check_passes_host_packed(gss_engine *eng, int n_passes, const uint32_t *const *states, int64_t n_vars,
+                                 int n_words, const uint32_t *start, const int32_t *solver_of_word,
+                                 gss_report_packed *const *outs, const int64_t *caps, int64_t *n_reports);
 
 /* ---- allocation-free check pass ----
  * No counterpart in the reference. For callers that cannot allocate device

@@ -151,9 +151,11 @@ def test_pass_through_host_buffers(engine):
     _assert_same(rep, ref, wl)
 
 
-def test_pipelined_passes_through_host_buffers(engine):
+@pytest.mark.parametrize("packed", [False, True])
+def test_pipelined_passes_through_host_buffers(engine, packed):
     """Several passes with different states, pipelined over three streams, each
-    equal to the oracle; small output capacities force the overflow path."""
+    equal to the oracle; small output capacities force the overflow path.
+    Packed: the 12-byte records packed on the device."""
     import gpusharesat_gb300 as g
     rng = np.random.default_rng(17)
     base = W.make_scale(seed=17, n_vars=2 ** 12, n_clauses=30000, n_solvers=32)
@@ -161,7 +163,7 @@ def test_pipelined_passes_through_host_buffers(engine):
     engine.set_db(base.lits, base.offsets)
     for caps in (None, [100] * 5):
         engine.set_capacity(0 if caps is None else 50)
-        got = g.passes_host(engine, states, base.start, base.solver_of_word, caps=caps)
+        got = g.passes_host(engine, states, base.start, base.solver_of_word, caps=caps, packed=packed)
         for st, rep in zip(states, got):
             ref = oracle.check(base.lits, base.offsets, st, base.start)
             _assert_same(g.sort_reports(rep), ref)
