@@ -577,6 +577,7 @@ def _sharer_sigs(lib):
     _sig(lib, "gss_sharer_set_max_clause_len", c_int, vp, c_int)
     _sig(lib, "gss_sharer_set_variant", c_int, vp, c_int, c_int, c_int, c_int)
     _sig(lib, "gss_sharer_set_clause_budget", c_int, vp, c_i64)
+    _sig(lib, "gss_sharer_set_locality", c_int, vp, c_int)
     _sig(lib, "gss_sharer_evicted_count", c_i64, vp)
     _sig(lib, "gss_sharer_device_compactions", c_i64, vp)
     _sig(lib, "gss_serving_run", c_int, vp, vp)
@@ -740,7 +741,7 @@ class ServingParams(ctypes.Structure):
                 ("budget", ctypes.c_int64), ("initial_clauses", ctypes.c_int64),
                 ("clause_rate", ctypes.c_double), ("plant_rate", ctypes.c_double),
                 ("batch_max", ctypes.c_int), ("trail_fraction", ctypes.c_double),
-                ("trail_change", ctypes.c_int), ("seed", ctypes.c_uint64)]
+                ("trail_change", ctypes.c_int), ("seed", ctypes.c_uint64), ("plain_scan", ctypes.c_int)]
 
 
 class ServingResult(ctypes.Structure):

@@ -27,7 +27,10 @@ serving: 2^21 variables; 64 solver threads with trails of half the variables
     of 2e5 clauses/s (lengths 1 + Zipf(1.2), at most 256; 0.05% planted to
     report) flows into an HBM budget of 16e6 clauses, full from the start.
     Reports p50/p99/p999 latency from an assignment's arrival to the moment
-    every report of it is delivered, and sustained checks/s.
+    every report of it is delivered, and sustained checks/s, for the sharer's
+    default form (persistent kernel over the variable-range order) and, with
+    --compare-plain 1, for the plain single-launch scan (grid-stride wide
+    kernel, length order) at the same rates.
 
 learned: 2^21 variables; 4e6 clauses at the start (lengths 1 + Zipf(1.2),
     at most 256) plus a stream of 500 new clauses per pass (as many of the
@@ -36,9 +39,12 @@ learned: 2^21 variables; 4e6 clauses at the start (lengths 1 + Zipf(1.2),
     planted; clause c is planted in a pass with latent probability
     r_c ~ Beta(0.5, 20), and its LBD falls with r_c. The order retrains every
     1000 passes; the head (delivered early) is the first 25% of the scan.
-    Reports the share of report bits in the first 10% of the learned scan
-    against the plain order's first 10%, the delivery latency of report bits
-    (from the launch call to the moment the host has them), and that each
+    The ordered passes run the persistent kernel (head and tail launches);
+    every compare_every passes the plain single launch (grid-stride wide
+    kernel, no order) checks the same state. Reports the share of report
+    bits in the first 10% of the learned scan against the plain order's
+    first 10%, the delivery latency of report bits (from the launch call to
+    the moment the host has them), checks/s of both forms, and that each
     compared pass reports what the plain scan reports.
 """
 import argparse
@@ -181,20 +187,28 @@ def serving(args):
     assignments at an aggregate rate, a clause stream into an HBM budget.
     Each rate is a fresh sharer with the same seed."""
     rows = []
+    plain_rows = []
     for rate in args.rates:
-        t0 = time.time()
-        r = g.serving_run(seconds=args.seconds, warmup_seconds=args.warmup_seconds, assign_rate=rate,
-                          n_solvers=64, n_vars=2 ** 21, budget=args.budget, initial_clauses=args.budget,
-                          clause_rate=2e5, plant_rate=0.0005, batch_max=32, trail_fraction=0.5,
-                          trail_change=8, seed=3)
-        r.update({"config": "serving", "assign_rate": rate, "budget": args.budget,
-                  "wall_s": round(time.time() - t0, 1)})
-        rows.append(r)
-        print(json.dumps(r), flush=True)
+        for plain in ((0, 1) if args.compare_plain else (0,)):
+            t0 = time.time()
+            r = g.serving_run(seconds=args.seconds, warmup_seconds=args.warmup_seconds, assign_rate=rate,
+                              n_solvers=64, n_vars=2 ** 21, budget=args.budget, initial_clauses=args.budget,
+                              clause_rate=2e5, plant_rate=0.0005, batch_max=32, trail_fraction=0.5,
+                              trail_change=8, seed=3, plain_scan=plain)
+            r.update({"config": "serving", "assign_rate": rate, "budget": args.budget,
+                      "form": "plain single launch (grid-stride wide kernel, length order)" if plain
+                      else "persistent kernel over the variable-range order, two-pass pipeline",
+                      "wall_s": round(time.time() - t0, 1)})
+            (plain_rows if plain else rows).append(r)
+            print(json.dumps(r), flush=True)
     summary = {"config": "serving", "rates": args.rates,
                "p50_ms": [r["p50_ms"] for r in rows], "p99_ms": [r["p99_ms"] for r in rows],
                "p999_ms": [r["p999_ms"] for r in rows], "checks_per_s": [r["checks_per_s"] for r in rows],
                "assignments_per_s": [r["assignments_per_s"] for r in rows]}
+    if plain_rows:
+        summary["plain"] = {"p50_ms": [r["p50_ms"] for r in plain_rows], "p99_ms": [r["p99_ms"] for r in plain_rows],
+                            "p999_ms": [r["p999_ms"] for r in plain_rows],
+                            "checks_per_s": [r["checks_per_s"] for r in plain_rows]}
     print(json.dumps(summary), flush=True)
     return summary
 
@@ -241,6 +255,12 @@ def learned(args):
     state = base.clone()
     start = torch.full((n_words,), -1, dtype=torch.int32, device=dev)
     eng = g.Engine(0)
+    # the composed form: the persistent kernel under the learned order; the
+    # comparison pass: the plain single launch (grid-stride wide kernel) on
+    # the same database and state (the state layout is the same for both)
+    composed = (g.KERNEL_WIDE4, 8, 2, g.VARIANT_PERSISTENT)
+    plain_variant = (g.KERNEL_WIDE4, 8, 2, 0)
+    eng.set_variant(*composed)
     eng.set_db(lits[:offsets[n0]], offsets[:n0 + 1])
     eng.order_enable(head_fraction=args.head_fraction, retrain_interval=args.retrain, train_epochs=2, seed=4,
                      overlap=args.overlap)
@@ -279,6 +299,7 @@ def learned(args):
                "tail_dev_ms": st["tail_ms"], "trainings": st["trainings"]}
         if p % args.compare_every == 0:
             eng.order_set_active(False)
+            eng.set_variant(*plain_variant)
             eng.set_timing(True)
             eng.kernel_time()
             td = time.perf_counter()
@@ -288,6 +309,7 @@ def learned(args):
             row["plain_all_ms"] = (te - td) * 1e3
             row["plain_dev_ms"] = eng.kernel_time()[0]
             eng.set_timing(False)
+            eng.set_variant(*composed)
             eng.order_set_active(True)
             def key(r):
                 o = np.lexsort((r["mask"], r["word"], r["clause"]))
@@ -358,6 +380,8 @@ def main(argv=None):
     p.add_argument("--head-fraction", type=float, default=0.25)
     p.add_argument("--compare-every", type=int, default=5)
     p.add_argument("--overlap", type=int, default=1)
+    p.add_argument("--compare-plain", type=int, default=1,
+                   help="serving: also run each rate with the plain single-launch scan")
     args = p.parse_args(argv)
     if args.config == "learned" and "--clauses" not in (argv or sys.argv):
         args.clauses = 4_000_000

@@ -133,6 +133,10 @@ int gss_serving_run(const gss_serving_params *p, gss_serving_result *res) {
     gss_sharer_set_cpu_solver_count(sh, p->n_solvers);
     gss_sharer_set_max_clause_len(sh, 256);
     gss_sharer_set_clause_budget(sh, p->budget);
+    if (p->plain_scan) {
+        gss_sharer_set_variant(sh, GSS_KERNEL_WIDE4, 8, 2, 0);
+        gss_sharer_set_locality(sh, 0);
+    }
     const LengthTable lt(1.2, 256);
     std::vector<uint8_t> model(p->n_vars);
     {

@@ -733,7 +733,7 @@ int Sharer::append_clauses(std::vector<int64_t> &ids, std::vector<int32_t> &lits
     // range, length) with each clause's device literals grouped by range, as
     // the engine's database order (range_order_key). The host arena keeps
     // the literals as the solver gave them, for delivery.
-    const int shift = range_shift_for(max_var_, -1);
+    const int shift = range_shift_for(max_var_, range_log2_);
     std::vector<uint64_t> key(ids.size());
     std::vector<int32_t> relits(shift ? lits.size() : 0);
     for (size_t i = 0; i < ids.size(); i++)
@@ -1211,7 +1211,7 @@ int Sharer::reduce_now(bool on_device) {
     act_->compact(keep);
     // the kept clauses in the device order of appended batches (length, or
     // variable range, second range, length)
-    const int shift = range_shift_for(max_var_, -1);
+    const int shift = range_shift_for(max_var_, range_log2_);
     std::vector<uint64_t> key(kept.size());
     for (size_t k = 0; k < kept.size(); k++)
         key[k] = shift ? range_order_key(&h_lits_[kept[k].lit_off], kept[k].len, shift, nullptr) : kept[k].len;
@@ -1490,6 +1490,14 @@ int gss_sharer_set_clause_budget(gss_sharer *s, int64_t max_clauses) {
 
 int64_t gss_sharer_evicted_count(gss_sharer *s) { return s ? s->impl->evicted() : -1; }
 int64_t gss_sharer_device_compactions(gss_sharer *s) { return s ? s->impl->device_compactions() : -1; }
+
+int gss_sharer_set_locality(gss_sharer *s, int range_log2) {
+    if (!s) return gss::set_error(GSS_ERR_INVALID, "sharer is NULL");
+    if (range_log2 != -1 && range_log2 != 0 && (range_log2 < 11 || range_log2 > 31))
+        return gss::set_error(GSS_ERR_INVALID, "range_log2 must be -1 (automatic), 0 (off) or 11..31, not %d", range_log2);
+    s->impl->set_locality(range_log2);
+    return GSS_OK;
+}
 
 int gss_sharer_set_variant(gss_sharer *s, int kind, int lanes_per_clause, int depth, int flags) {
     GSS_SHARER(s);

@@ -160,6 +160,9 @@ public:
     void set_max_clause_len(int n) { max_len_ = n; }
     int set_variant(int kind, int lpc, int depth, int flags);
     void set_clause_budget(int64_t n) { budget_ = n; }
+    // device order of appended batches and reduceDb survivors: variable
+    // ranges of 2^r (-1: automatic, 0: length order), as gss_db_set_locality
+    void set_locality(int r) { range_log2_ = r; }
     int64_t evicted() const { return evicted_; }
     int64_t device_compactions() const { return device_compactions_; }
     int64_t live_clauses() const { return (int64_t) meta_.size() - n_dead_; }
@@ -212,6 +215,7 @@ private:
     int device_ = 0, sm_count_ = 0;
     cudaStream_t stream_ = nullptr;
     int max_len_ = 100;  // MAX_CL_SIZE, gpuShareLib/BaseTypes.cuh:28
+    int range_log2_ = -1;
 
     // statistics
     std::vector<std::atomic<int64_t>> stats_;

@@ -462,6 +462,10 @@ int64_t gss_sharer_evicted_count(gss_sharer *s);
  * clauses on the GPU. */
 int64_t gss_sharer_device_compactions(gss_sharer *s);
 int gss_sharer_set_variant(gss_sharer *s, int kind, int lanes_per_clause, int depth, int flags);
+/* Device order of the sharer's database, as gss_db_set_locality (-1
+ * automatic variable ranges, 0 length order, 11..31); applies to batches
+ * appended from then on and to reduceDb. No counterpart in the reference. */
+int gss_sharer_set_locality(gss_sharer *s, int range_log2);
 
 /* ---- serving load generator (no counterpart in the reference) ----
  * Simulated solver threads drive one sharer on the calling thread's current
@@ -484,6 +488,8 @@ typedef struct gss_serving_params {
     double trail_fraction;     /* initial trail length / n_vars */
     int trail_change;          /* an assignment unsets and sets 1..trail_change literals */
     uint64_t seed;
+    int plain_scan;            /* 1: the plain single-launch scan (grid-stride wide kernel, length order)
+                                  instead of the automatic persistent kernel over the range order */
 } gss_serving_params;
 
 typedef struct gss_serving_result {
