@@ -118,7 +118,7 @@ def load_traffic():
     workload, from the committed ncu summary (its `traffic_bytes_per_launch`
     line), or None."""
     import re
-    path = os.path.join(ROOT, "profiles", "check_wide_kernel_plain_scale.md")
+    path = os.path.join(ROOT, "profiles", "check_wide_persist_kernel_plain_scale.md")
     if os.path.exists(path):
         with open(path) as f:
             m = re.search(r"traffic_bytes_per_launch:\s*([0-9]+)", f.read())
@@ -418,7 +418,8 @@ def run_gpu(args):
                     "frac": achieved / peak,
                     "traffic": traffic,
                     "traffic_source": ("ncu capture of this kernel on this workload, committed summary "
-                                       "profiles/check_wide_kernel_plain_scale.md (not measured in this run)")
+                                       "profiles/check_wide_persist_kernel_plain_scale.md (not measured in this "
+                                       "run)")
                     if traffic else None,
                     "algorithmic_bytes_per_launch": B, "kernel_ms": kern_avg_s * 1e3,
                     "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
