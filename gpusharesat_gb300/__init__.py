@@ -751,7 +751,10 @@ class ServingResult(ctypes.Structure):
                 ("checks_per_s", ctypes.c_double), ("assignments_per_s", ctypes.c_double),
                 ("elapsed_s", ctypes.c_double), ("evicted", ctypes.c_int64), ("retries", ctypes.c_int64),
                 ("clauses_streamed", ctypes.c_int64), ("live_clauses_end", ctypes.c_int64),
-                ("device_compactions", ctypes.c_int64)]
+                ("device_compactions", ctypes.c_int64), ("run_ms_p50", ctypes.c_double),
+                ("run_ms_p99", ctypes.c_double), ("run_ms_max", ctypes.c_double), ("long_runs", ctypes.c_int64),
+                ("long_wait_ms", ctypes.c_double), ("long_launch_ms", ctypes.c_double),
+                ("long_deliver_ms", ctypes.c_double), ("long_other_ms", ctypes.c_double)]
 
 
 def serving_run(**params):

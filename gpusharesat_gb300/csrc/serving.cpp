@@ -215,6 +215,8 @@ int gss_serving_run(const gss_serving_params *p, gss_serving_result *res) {
     std::mutex measure_lock;
 
     // GPU thread: clause stream and passes
+    std::vector<float> run_ms;  // gpuRun call durations in the measured window (GPU thread only)
+    double long_ms[4] = {0, 0, 0, 0};
     std::thread gpu([&]() {
         Rng r(p->seed * 31 + 5);
         ClauseGen gen(lt, model);
@@ -259,7 +261,26 @@ int gss_serving_run(const gss_serving_params *p, gss_serving_result *res) {
                 if (!cl.empty()) gss_sharer_add_clause(sh, -1, cl.data(), (int) cl.size());
             }
             streamed = produced;
-            if (gss_sharer_gpu_run(sh) != GSS_OK) {
+            const double r0 = now_s(t0);
+            // the sharer's time statistics (microseconds): timeSpentTestingClauses (9),
+            // timeSpentFillingAssigs (10), timeSpentFillingReported (11)
+            int64_t st0[3];
+            for (int k = 0; k < 3; k++) st0[k] = gss_sharer_global_stat(sh, 9 + k);
+            const int rc_run = gss_sharer_gpu_run(sh);
+            if (r0 >= t_measure && r0 < t_end) {
+                const double ms = (now_s(t0) - r0) * 1e3;
+                run_ms.push_back((float) ms);
+                if (ms > 20.0) {
+                    double parts = 0;
+                    for (int k = 0; k < 3; k++) {
+                        const double d = (gss_sharer_global_stat(sh, 9 + k) - st0[k]) * 1e-3;
+                        long_ms[k] += d;
+                        parts += d;
+                    }
+                    long_ms[3] += ms - parts;
+                }
+            }
+            if (rc_run != GSS_OK) {
                 gpu_error = 1;
                 stop = true;
                 notify_pass();
@@ -395,6 +416,17 @@ int gss_serving_run(const gss_serving_params *p, gss_serving_result *res) {
     res->clauses_streamed = streamed;
     res->live_clauses_end = gss_sharer_global_stat(sh, 0 /* gpuClauses */);
     res->device_compactions = gss_sharer_device_compactions(sh);
+    std::sort(run_ms.begin(), run_ms.end());
+    if (!run_ms.empty()) {
+        res->run_ms_p50 = run_ms[(size_t) (0.5 * (run_ms.size() - 1))];
+        res->run_ms_p99 = run_ms[(size_t) (0.99 * (run_ms.size() - 1))];
+        res->run_ms_max = run_ms.back();
+        for (float x : run_ms) res->long_runs += x > 20.0f;
+    }
+    res->long_wait_ms = long_ms[0];
+    res->long_launch_ms = long_ms[1];
+    res->long_deliver_ms = long_ms[2];
+    res->long_other_ms = long_ms[3];
     gss_sharer_destroy(sh);
     return gpu_error ? GSS_ERR_CUDA : GSS_OK;
 }

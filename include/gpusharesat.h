@@ -505,6 +505,12 @@ typedef struct gss_serving_result {
     int64_t clauses_streamed;
     int64_t live_clauses_end;
     int64_t device_compactions;
+    double run_ms_p50, run_ms_p99, run_ms_max;  /* gpuRun call durations in the measured window */
+    int64_t long_runs;         /* gpuRun calls in the measured window that took more than 20 ms */
+    /* where those long calls spent their time (ms, summed): waiting for the
+     * pass on the GPU, cutting and launching the next, delivering reports,
+     * the rest (appending clauses, eviction, compaction) */
+    double long_wait_ms, long_launch_ms, long_deliver_ms, long_other_ms;
 } gss_serving_result;
 
 int gss_serving_run(const gss_serving_params *p, gss_serving_result *res);
