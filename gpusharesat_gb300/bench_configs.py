@@ -265,7 +265,8 @@ def learned(args):
     eng.order_enable(head_fraction=args.head_fraction, retrain_interval=args.retrain, train_epochs=2, seed=4,
                      overlap=args.overlap)
     eng.set_lbd(np.arange(n0, dtype=np.uint32), d["lbd"][:n0])
-    eng.set_capacity(1 << 22)
+    # room for the planted reports of a pass (about 0.75 records per clause at 64 words)
+    eng.set_capacity(max(1 << 22, 2 * n0))
     lo, nxt = 0, n0
     rows = []
     # report buffers reused across passes (their pages stay mapped)

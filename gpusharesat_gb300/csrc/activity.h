@@ -36,6 +36,11 @@ public:
     // Reorders the entries from `first` on: new entry first + k is old entry
     // first + order[k].
     void permute_tail(size_t first, const std::vector<uint32_t> &order);
+    // room for n clauses without reallocating
+    void reserve(size_t n) {
+        act_.reserve(n);
+        lbd_.reserve(n);
+    }
 
     // An approximation, from above, of the n-th lowest activity among entries
     // with min_lbd <= lbd < max_lbd (20000 logarithmic buckets). 0 for n = 0;

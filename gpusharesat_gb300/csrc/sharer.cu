@@ -701,6 +701,36 @@ int Sharer::compact(bool upload, std::vector<uint32_t> *old_index) {
     return GSS_OK;
 }
 
+void Sharer::reserve_for_budget(size_t n_new, size_t n_new_lits) {
+    // Under an HBM budget the database streams: clauses come in, the oldest
+    // leave as tombstones. Host arrays hold up to twice the budget before a
+    // host compaction, device arrays about 1.25 times before a device one.
+    // Growing those arrays by doubling in the middle of serving stalls one
+    // pass for tens of milliseconds (a 400 MB host copy at 2^24 clauses), so
+    // their room is set aside once, the first time the budget is in force.
+    if (budget_ <= 0 || reserved_for_ >= budget_) return;
+    const size_t host_clauses = (size_t) (2 * budget_) + n_new + 4096;
+    meta_.reserve(host_clauses);
+    act_->reserve(host_clauses);
+    h_alive_.reserve((host_clauses + 31) / 32);
+    const size_t dev_clauses = (size_t) (budget_ + budget_ / 4) + n_new + 4096;
+    const double mean_len = (double) (stats_[kGpuClauseLengthSum] + (int64_t) n_new_lits) /
+                            (double) std::max<int64_t>(stats_[kGpuClauses] + (int64_t) n_new, 1);
+    const size_t dev_lits = (size_t) (mean_len * (double) dev_clauses * 1.1) + kClausePad;
+    h_lits_.reserve(h_lits_.size() + (size_t) (mean_len * (double) budget_) + n_new_lits);
+    // best effort: without the device room, the arrays grow when needed (and
+    // a failure there takes the out-of-memory path)
+    if (d_lits_.grow_keep(dev_lits * sizeof(int32_t), stream_, (size_t) dev_lits_ * sizeof(int32_t)) == GSS_OK &&
+        d_offsets_.grow_keep((dev_clauses + 1) * sizeof(int64_t), stream_,
+                             (size_t) (dev_clauses_ ? dev_clauses_ + 1 : 0) * sizeof(int64_t)) == GSS_OK &&
+        d_orig_.grow_keep(dev_clauses * sizeof(uint32_t), stream_, (size_t) dev_clauses_ * sizeof(uint32_t)) ==
+            GSS_OK) {
+        d_alive_.grow_keep((host_clauses + 31) / 32 * sizeof(uint32_t), stream_,
+                           alive_synced_ ? std::min(d_alive_.bytes, (host_clauses + 31) / 32 * sizeof(uint32_t)) : 0);
+    }
+    reserved_for_ = budget_;
+}
+
 int Sharer::append_clauses(std::vector<int64_t> &ids, std::vector<int32_t> &lits, std::vector<uint32_t> &lens) {
     // HostClauses::getUpdatesForDevice (gpuShareLib/Clauses.cu:318-346): per
     // new clause, decay the activity increment, then give the clause that
@@ -715,6 +745,7 @@ int Sharer::append_clauses(std::vector<int64_t> &ids, std::vector<int32_t> &lits
         off += lens[i];
     }
     for (int32_t l : lits) max_var_ = std::max<int64_t>(max_var_, (int64_t) (l >> 1));
+    reserve_for_budget(ids.size(), lits.size());
     for (size_t i = 0; i < ids.size(); i++) {
         // the API carries no LBD: LBD := length (GpuClauseSharerImpl.cu:125)
         act_->add((int) lens[i]);

@@ -201,6 +201,7 @@ private:
     int run_check(Pass &p);
     int ensure_state();
     int append_clauses(std::vector<int64_t> &ids, std::vector<int32_t> &lits, std::vector<uint32_t> &lens);
+    void reserve_for_budget(size_t n_new, size_t n_new_lits);
     int upload_db();
     void evict(int64_t n);
     int compact(bool upload = true, std::vector<uint32_t> *old_index = nullptr);
@@ -250,6 +251,7 @@ private:
     // bitmap and dropped by compact_device() once evicted clauses are a fifth
     // of the device database.
     int64_t budget_ = 0;
+    int64_t reserved_for_ = 0;  // the budget whose room reserve_for_budget set aside
     int64_t evicted_ = 0;
     int64_t n_dead_ = 0;     // tombstones in meta_
     int64_t dev_dead_ = 0;   // evicted clauses still in the device arrays
