@@ -159,7 +159,7 @@ __device__ __forceinline__ void range_task(const CheckArgs &a, uint32_t blk, uin
     }
 }
 
-__global__ void __launch_bounds__(kWarps * 32, 1) check_bucketed_kernel(const CheckArgs *__restrict__ pa,
+__global__ void __launch_bounds__(kWarps * 32, 6) check_bucketed_kernel(const CheckArgs *__restrict__ pa,
                                                                         const BucketPlan *__restrict__ plan,
                                                                         uint32_t *__restrict__ work) {
     __shared__ CheckArgs sa;
