@@ -228,7 +228,7 @@ int gss_engine_destroy(gss_engine *eng) {
     if (eng->graph) cudaGraphDestroy(eng->graph);
     if (eng->h2d) cudaStreamDestroy(eng->h2d);
     if (eng->d2h) cudaStreamDestroy(eng->d2h);
-    for (int b = 0; b < 2; b++) {
+    for (int b = 0; b < 3; b++) {
         if (eng->ev_h2d[b]) cudaEventDestroy(eng->ev_h2d[b]);
         if (eng->ev_kernel[b]) cudaEventDestroy(eng->ev_kernel[b]);
         if (eng->ev_d2h[b]) cudaEventDestroy(eng->ev_d2h[b]);
@@ -1074,8 +1074,9 @@ int passes_host(gss_engine *eng, int n_passes, const uint32_t *const *states, in
                 int64_t *n_reports, bool packed) {
     // Passes i = 0..n-1 over three streams: the state of pass i+1 goes
     // host->device (h2d stream) and the reports of pass i-1 come back (d2h
-    // stream) while pass i runs (engine stream). Double buffers: state b and
-    // report set b belong to passes b, b+2, b+4...
+    // stream) while pass i runs (engine stream). Three buffer slots: state b
+    // and report set b belong to passes b, b+3, b+6..., so a copy waits for
+    // the pass three back, not the one just before.
     if (!eng || n_passes < 0 || (n_passes > 0 && (!states || !outs || !caps || !n_reports)))
         return set_error(GSS_ERR_INVALID, "bad arguments to gss_check_passes_host");
     if (n_passes == 0) return GSS_OK;
@@ -1088,20 +1089,29 @@ int passes_host(gss_engine *eng, int n_passes, const uint32_t *const *states, in
     const size_t bbytes = (size_t) eng->n_blocks * n_vars * eng->state_bw * sizeof(uint2);
     if (!eng->h2d) GSS_CUDA_TRY(cudaStreamCreateWithFlags(&eng->h2d, cudaStreamNonBlocking));
     if (!eng->d2h) GSS_CUDA_TRY(cudaStreamCreateWithFlags(&eng->d2h, cudaStreamNonBlocking));
-    for (int b = 0; b < 2; b++) {
+    constexpr int NB = 3;
+    for (int b = 0; b < NB; b++) {
         if (!eng->ev_h2d[b]) GSS_CUDA_TRY(cudaEventCreateWithFlags(&eng->ev_h2d[b], cudaEventDisableTiming));
         if (!eng->ev_kernel[b]) GSS_CUDA_TRY(cudaEventCreateWithFlags(&eng->ev_kernel[b], cudaEventDisableTiming));
         if (!eng->ev_d2h[b]) GSS_CUDA_TRY(cudaEventCreateWithFlags(&eng->ev_d2h[b], cudaEventDisableTiming));
     }
     GSS_TRY(eng->state2.reserve(std::max<size_t>(bbytes, 8)));
+    GSS_TRY(eng->state3.reserve(std::max<size_t>(bbytes, 8)));
     if (!direct) {
         GSS_TRY(eng->state_raw.reserve(std::max<size_t>(sbytes, 8)));
         GSS_TRY(eng->state_raw2.reserve(std::max<size_t>(sbytes, 8)));
+        GSS_TRY(eng->state_raw3.reserve(std::max<size_t>(sbytes, 8)));
     }
-    GSS_TRY(eng->reports2.reserve((size_t) eng->cap_per_part * eng->n_parts * sizeof(gss_report)));
+    auto reserve_reports = [&]() -> int {
+        GSS_TRY(eng->reports2.reserve((size_t) eng->cap_per_part * eng->n_parts * sizeof(gss_report)));
+        GSS_TRY(eng->reports3.reserve((size_t) eng->cap_per_part * eng->n_parts * sizeof(gss_report)));
+        return GSS_OK;
+    };
+    GSS_TRY(reserve_reports());
     GSS_TRY(eng->counts2.reserve(sizeof(uint32_t) * eng->n_parts));
+    GSS_TRY(eng->counts3.reserve(sizeof(uint32_t) * eng->n_parts));
     auto reserve_packed = [&]() -> int {
-        for (int b = 0; b < 2 && packed; b++)
+        for (int b = 0; b < NB && packed; b++)
             GSS_TRY(eng->packed[b].reserve((size_t) eng->cap_per_part * eng->n_parts * 3 * sizeof(uint32_t)));
         return GSS_OK;
     };
@@ -1113,17 +1123,18 @@ int passes_host(gss_engine *eng, int n_passes, const uint32_t *const *states, in
                                    eng->cap_per_part, (uint32_t *) eng->packed[b].ptr, eng->stream, eng->sm_count);
     };
     GSS_TRY(eng->h_counts2.reserve(sizeof(uint32_t) * (eng->n_parts + 1)));
-    DevBuf *state_buf[2] = {&eng->state, &eng->state2};
-    DevBuf *raw_buf[2] = {&eng->state_raw, &eng->state_raw2};
-    DevBuf *rep_buf[2] = {&eng->reports, &eng->reports2};
-    DevBuf *cnt_buf[2] = {&eng->counts, &eng->counts2};
-    PinnedBuf *hcnt_buf[2] = {&eng->h_counts, &eng->h_counts2};
+    GSS_TRY(eng->h_counts3.reserve(sizeof(uint32_t) * (eng->n_parts + 1)));
+    DevBuf *state_buf[NB] = {&eng->state, &eng->state2, &eng->state3};
+    DevBuf *raw_buf[NB] = {&eng->state_raw, &eng->state_raw2, &eng->state_raw3};
+    DevBuf *rep_buf[NB] = {&eng->reports, &eng->reports2, &eng->reports3};
+    DevBuf *cnt_buf[NB] = {&eng->counts, &eng->counts2, &eng->counts3};
+    PinnedBuf *hcnt_buf[NB] = {&eng->h_counts, &eng->h_counts2, &eng->h_counts3};
     GSS_CUDA_TRY(cudaStreamSynchronize(eng->stream));  // pass 0's state is in buffer 0
 
     int launched = 0;
     // copies the reports of pass j back (the host waits for its kernel)
     auto finish = [&](int j) -> int {
-        const int b = j & 1;
+        const int b = j % NB;
         GSS_CUDA_TRY(cudaEventSynchronize(eng->ev_kernel[b]));
         const uint32_t *hc = (const uint32_t *) hcnt_buf[b]->ptr;
         if (hc[eng->n_parts] != 0)
@@ -1142,14 +1153,14 @@ int passes_host(gss_engine *eng, int n_passes, const uint32_t *const *states, in
             GSS_CUDA_TRY(cudaDeviceSynchronize());
             eng->requested_cap = std::max<int64_t>(eng->requested_cap, total * 2 + eng->n_parts * 1024);
             GSS_TRY(ensure_queues(eng));
-            GSS_TRY(eng->reports2.reserve((size_t) eng->cap_per_part * eng->n_parts * sizeof(gss_report)));
+            GSS_TRY(reserve_reports());
             GSS_TRY(reserve_packed());
             GSS_TRY(launch_pass_into(eng, state_buf[b]->ptr, *rep_buf[b], *cnt_buf[b], *hcnt_buf[b]));
             GSS_TRY(pack(b, *rep_buf[b], *cnt_buf[b]));
             eng->launches++;
             GSS_CUDA_TRY(cudaEventRecord(eng->ev_kernel[b], eng->stream));
             if (j + 1 < launched) {
-                const int nb = b ^ 1;
+                const int nb = (j + 1) % NB;
                 GSS_TRY(launch_pass_into(eng, state_buf[nb]->ptr, *rep_buf[nb], *cnt_buf[nb], *hcnt_buf[nb]));
                 GSS_TRY(pack(nb, *rep_buf[nb], *cnt_buf[nb]));
                 eng->launches++;
@@ -1183,10 +1194,10 @@ int passes_host(gss_engine *eng, int n_passes, const uint32_t *const *states, in
 
     auto pipeline = [&]() -> int {
     for (int i = 0; i < n_passes; i++) {
-        const int b = i & 1;
+        const int b = i % NB;
         if (i > 0) {
-            // state i -> buffer b, once pass i-2 (the last reader of b) is done
-            if (i >= 2) GSS_CUDA_TRY(cudaStreamWaitEvent(eng->h2d, eng->ev_kernel[b], 0));
+            // state i -> buffer b, once pass i-3 (the last reader of b) is done
+            if (i >= NB) GSS_CUDA_TRY(cudaStreamWaitEvent(eng->h2d, eng->ev_kernel[b], 0));
             void *dst = direct ? state_buf[b]->ptr : raw_buf[b]->ptr;
             if (!states[i]) return set_error(GSS_ERR_INVALID, "state %d is NULL", i);
             GSS_CUDA_TRY(cudaMemcpyAsync(dst, states[i], sbytes, cudaMemcpyHostToDevice, eng->h2d));
@@ -1197,8 +1208,8 @@ int passes_host(gss_engine *eng, int n_passes, const uint32_t *const *states, in
                                         (uint32_t) n_words, (uint32_t) eng->state_bw, (uint32_t) eng->n_blocks,
                                         eng->stream, eng->sm_count));
         }
-        // report set b is free once pass i-2's reports are back
-        if (i >= 2) GSS_CUDA_TRY(cudaStreamWaitEvent(eng->stream, eng->ev_d2h[b], 0));
+        // report set b is free once pass i-3's reports are back
+        if (i >= NB) GSS_CUDA_TRY(cudaStreamWaitEvent(eng->stream, eng->ev_d2h[b], 0));
         GSS_TRY(launch_pass_into(eng, state_buf[b]->ptr, *rep_buf[b], *cnt_buf[b], *hcnt_buf[b]));
         GSS_TRY(pack(b, *rep_buf[b], *cnt_buf[b]));
         eng->launches++;

@@ -72,11 +72,13 @@ struct gss_engine {
 
     // pipelined passes through host buffers (gss_check_passes_host): second
     // state and report buffers, copy streams and events
+    // slots 1 and 2 of the three-slot pipeline (slot 0 is the engine's own)
     DevBuf state2, state_raw2, reports2, counts2;
-    DevBuf packed[2];  // 12-byte records of gss_check_passes_host_packed
-    PinnedBuf h_counts2;
+    DevBuf state3, state_raw3, reports3, counts3;
+    DevBuf packed[3];  // 12-byte records of gss_check_passes_host_packed
+    PinnedBuf h_counts2, h_counts3;
     cudaStream_t h2d = nullptr, d2h = nullptr;
-    cudaEvent_t ev_h2d[2] = {nullptr, nullptr}, ev_kernel[2] = {nullptr, nullptr}, ev_d2h[2] = {nullptr, nullptr};
+    cudaEvent_t ev_h2d[3] = {}, ev_kernel[3] = {}, ev_d2h[3] = {};
 
     // persistent kernel: arguments in device memory, task counter; optional
     // CUDA graph of a pass (memsets, kernel, count readback), recaptured when
