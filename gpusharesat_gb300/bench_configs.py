@@ -12,14 +12,15 @@ batching: 8e6 clauses (lengths 1 + Zipf(1.2), at most 256), 48 solvers sending
     uneven batches of 4..64 assignments per pass (two 32-slot words each), 5%
     clause churn per pass (deletes plus new clauses from the small workload's
     generator). Three ways to check a pass, all over the same database:
-      per_solver  one launch of the default kernel per solver's batch
-      single      one launch of the default kernel for all batches
+      per_solver  one launch of the grid-stride wide kernel per solver's batch
+      single      one launch of the grid-stride wide kernel for all batches
       batched     the autotuned persistent kernel for all batches, replayed
                   as a captured CUDA graph
       bucketed    the bucketed persistent kernel with a lane layout per
                   length class (tuned class by class), replayed as a graph
-    The reports of `batched` and `single` are compared record for record on
-    the first pass, and the union of the per-solver launches with `single`'s.
+    The report sets of `batched`, `bucketed` and `single`, and the union of
+    the per-solver launches, are compared on the first pass through an
+    order-independent hash sum of their (clause, word, mask) records.
 
 serving: 2^21 variables; 64 solver threads with trails of half the variables
     send assignments (each unsets and sets 1..8 literals) in Poisson batches
@@ -57,6 +58,28 @@ import numpy as np
 import gpusharesat_gb300 as g
 from gpusharesat_gb300 import autotune, build
 from gpusharesat_gb300 import workloads as W
+
+
+def _mix64(z):
+    z = z + np.uint64(0x9E3779B97F4A7C15)
+    z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+    z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    return z ^ (z >> np.uint64(31))
+
+
+def _digest(reps, chunk=1 << 24):
+    """(records, order-independent 64-bit hash sum) of one or more report
+    arrays, for comparing report sets of hundreds of millions of records
+    without sorting them."""
+    n, total = 0, np.uint64(0)
+    with np.errstate(over="ignore"):
+        for rep in reps:
+            for b in range(0, len(rep), chunk):
+                r = rep[b:b + chunk]
+                key = (r["clause"].astype(np.uint64) << np.uint64(32)) | r["word"].astype(np.uint64)
+                total = total + np.add.reduce(_mix64(_mix64(key) ^ r["mask"].astype(np.uint64)), dtype=np.uint64)
+            n += len(rep)
+    return n, int(total)
 
 
 def _sorted(rep):
@@ -121,8 +144,8 @@ def batching(args):
                 eng.compact()
         start, sizes = W.batch_starts(rng, wl.n_solvers)
         checks = len(live) * int(sizes.sum())
-        # single launch, default kernel
-        eng.set_variant()
+        # single launch: the plain grid-stride wide kernel
+        eng.set_variant(g.KERNEL_WIDE4, 8, 2, 0)
         eng.set_state(wl.state, start, wl.solver_of_word)
         ref = eng.check() if p == 0 else None
         single_ms = _timed(eng, eng.launch)
@@ -135,7 +158,7 @@ def batching(args):
                 m[2 * s:2 * s + 2] = start[2 * s:2 * s + 2]
                 eng.set_start(m)
                 if p == 0:
-                    per_solver_reps.append(eng.check())
+                    per_solver_reps.append(_digest([eng.check()]))
                 else:
                     eng.launch()
                     eng.wait()
@@ -161,9 +184,11 @@ def batching(args):
                "batched_checks_per_s": checks / (batched_ms / 1e3), "bucketed_ms": bucketed_ms,
                "bucketed_checks_per_s": checks / (bucketed_ms / 1e3), "graph_captures": eng.graph_captures}
         if p == 0:
-            row["batched_equals_single"] = _same(got, ref)
-            row["bucketed_equals_single"] = _same(got_b, ref)
-            row["per_solver_union_equals_single"] = _same(np.concatenate(per_solver_reps), ref)
+            dref = _digest([ref])
+            row["batched_equals_single"] = _digest([got]) == dref
+            row["bucketed_equals_single"] = _digest([got_b]) == dref
+            union = (sum(x[0] for x in per_solver_reps), int(sum(x[1] for x in per_solver_reps) % (1 << 64)))
+            row["per_solver_union_equals_single"] = union == dref
             row["reports"] = int(len(ref))
         rows.append(row)
         print(json.dumps(row), flush=True)
@@ -299,6 +324,9 @@ def learned(args):
                "all_ms": (tc - ta) * 1e3, "score_dev_ms": st["score_ms"], "head_dev_ms": st["head_ms"],
                "tail_dev_ms": st["tail_ms"], "trainings": st["trainings"]}
         if p % args.compare_every == 0:
+            # the plain pass starts on an idle GPU (the order's scoring of the
+            # next pass, on its own stream, is not charged to it)
+            torch.cuda.synchronize()
             eng.order_set_active(False)
             eng.set_variant(*plain_variant)
             eng.set_timing(True)
