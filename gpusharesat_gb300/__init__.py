@@ -721,6 +721,12 @@ class ClauseSharer:
     def setVariant(self, kind=-1, lanes_per_clause=0, depth=2, flags=0):
         _check(self.lib.gss_sharer_set_variant(self.h, kind, lanes_per_clause, depth, flags))
 
+    def setLocality(self, range_log2=-1):
+        """Device order of the database (gss_sharer_set_locality): -1
+        automatic variable ranges, 0 length order, 11..31 ranges of
+        2^range_log2 variables."""
+        _check(self.lib.gss_sharer_set_locality(self.h, int(range_log2)))
+
     def setClauseBudget(self, max_clauses):
         """HBM budget: a pass checks at most max_clauses live clauses; the
         oldest clauses not reported in the last 8 passes are evicted first.

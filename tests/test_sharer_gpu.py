@@ -451,3 +451,31 @@ def test_many_solvers_full_rings_match_oracle(lib):
     assert got == want
     assert s.getGlobalStat("gpuReports") == len(want)
     assert s.getGlobalStat("totalAssigClauseTested") == n_cl * 32 * n_solvers
+
+
+@pytest.mark.parametrize("locality", [0, 11])
+def test_range_order_reports_every_clause_with_the_solvers_literals(lib, locality):
+    """With the device database in variable-range order (8 ranges of 2^11
+    variables: device literals regrouped by range, clauses sorted by range)
+    or in length order, an all-false assignment reports every clause, each
+    handed back with its literals in the order the solver added them, and a
+    reduceDb (rebuilt on the device) keeps that."""
+    n_vars = 16384
+    s = make(lib, n_vars, 2)
+    s.setLocality(locality)
+    rng = np.random.default_rng(40 + locality)
+    added = {}
+    for k in range(3000):
+        L = int(rng.integers(1, 3))
+        vs = rng.choice(n_vars, size=L, replace=False)
+        cl = [lit(int(v)) for v in vs]
+        added[s.addClause(-1, cl)] = cl
+    s.gpuRun()  # uploads the database
+    for solver in (0, 1):
+        assert s.trySetSolverValues(solver, [lit(v, True) for v in range(n_vars)])
+        assert s.trySendAssignment(solver) >= 0
+        execute(s)
+        got = {c: list(l) for l, c in s.popAll(solver)}
+        assert got == added
+        if solver == 0:
+            s.reduceDb()  # unit and binary clauses: all kept
