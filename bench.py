@@ -8,11 +8,11 @@ those shapes (the reference publishes no dataset).
 
 value: checks/s with the clause database and the assignment planes resident
        in HBM (kernel passes back to back, CUDA events on the launch stream).
-e2e:   the same metric through the C ABI call gss_check_passes_host_packed
+e2e:   the same metric through the C ABI call gss_check_passes_host_cells
        with host buffers: every step's assignment planes go host->device from
-       pinned memory and its reports come back device->host as 12-byte
-       records; the copies of neighbouring steps overlap the current step's
-       check.
+       pinned memory and its reports come back device->host as 8-byte
+       records {clause * words + word, mask}; the copies of neighbouring
+       steps overlap the current step's check.
 latency: submit-to-report p50/p99/p999 through the GpuClauseSharer C ABI
        (the serving shape; see serving_leg).
 The inputs (about 0.6 GB) are larger than the 129 MB L2, so no flush is
@@ -381,7 +381,7 @@ def run_gpu(args):
     start_h = torch.from_numpy(wl.start).pin_memory()
     sow_h = torch.from_numpy(wl.solver_of_word).pin_memory()
     cap = n_reports + 1024
-    outs_h = [torch.empty(cap * 3, dtype=torch.int32).pin_memory() for _ in range(2)]
+    outs_h = [torch.empty(cap * 2, dtype=torch.int32).pin_memory() for _ in range(2)]
     lib = g.load()
 
     def e2e_run(k):
@@ -389,13 +389,14 @@ def run_gpu(args):
         op = (ctypes.c_void_p * k)(*[outs_h[i % 2].data_ptr() for i in range(k)])
         caps = (ctypes.c_int64 * k)(*([cap] * k))
         nrep = (ctypes.c_int64 * k)()
-        rc = lib.gss_check_passes_host_packed(eng.h, k, sp, wl.n_vars, wl.n_words,
-                                              ctypes.c_void_p(start_h.data_ptr()), ctypes.c_void_p(sow_h.data_ptr()),
-                                              op, caps, nrep)
+        rc = lib.gss_check_passes_host_cells(eng.h, k, sp, wl.n_vars, wl.n_words,
+                                             ctypes.c_void_p(start_h.data_ptr()), ctypes.c_void_p(sow_h.data_ptr()),
+                                             op, caps, nrep)
         g._check(rc)
         assert all(nrep[i] == n_reports for i in range(k)), list(nrep)
 
     e2e_s = float("nan")
+    e2e_parity = None
     if not args.no_e2e:
         e2e_run(max(2, args.warmup))
         barrier()
@@ -404,8 +405,15 @@ def run_gpu(args):
         e2e_run(args.e2e_steps)
         torch.cuda.synchronize()
         e2e_s = max_over_ranks((time.perf_counter() - t0) / args.e2e_steps, world, "cuda")
+        if rank == 0:
+            # the last timed step's host records against the sizing pass (outside the timed region)
+            cells = outs_h[(args.e2e_steps - 1) % 2].numpy().view(g.CELL_REPORT_DTYPE)[:n_reports]
+            got = g.sort_reports(g.cells_to_reports(cells, wl.n_words))
+            ref = g.sort_reports(sizing_reports)
+            e2e_parity = {"records": int(n_reports), "mismatches": int(
+                ((got["clause"] != ref["clause"]) | (got["word"] != ref["word"]) | (got["mask"] != ref["mask"])).sum())}
     h2d = wl.state.nbytes + wl.start.nbytes + wl.solver_of_word.nbytes
-    d2h = n_reports * 12 + 16 * 4  # packed {clause, word, mask} records, and the counters
+    d2h = n_reports * 8 + 16 * 4  # {clause * words + word, mask} records, and the counters
 
     if rank == 0:
         peak, peak_kind = load_peaks()
@@ -433,7 +441,9 @@ def run_gpu(args):
             "e2e": {"value": job_throughput(checks_per_pass, world, e2e_s), "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3,
                     "host_link_gbs": (h2d + d2h) / e2e_s / 1e9,
-                    "call": "gss_check_passes_host_packed (12-byte report records packed on the device)"}
+                    "call": "gss_check_passes_host_cells (8-byte {clause * words + word, mask} report records "
+                            "packed on the device)",
+                    "parity_vs_sizing_pass": e2e_parity}
             if not args.no_e2e else None,
             "database_order": {"locality_shift": eng.locality_shift},
             "roofline": roofline,

@@ -42,6 +42,7 @@ LAYOUTS = (LAYOUT_4x8_G1, LAYOUT_4x8_G2, LAYOUT_2x16_G1, LAYOUT_2x16_G2, LAYOUT_
 
 REPORT_DTYPE = np.dtype([("clause", "<u4"), ("word", "<u4"), ("mask", "<u4"), ("solver", "<u4")])
 PACKED_REPORT_DTYPE = np.dtype([("clause", "<u4"), ("word", "<u4"), ("mask", "<u4")])
+CELL_REPORT_DTYPE = np.dtype([("cell", "<u4"), ("mask", "<u4")])
 
 _lib = None
 
@@ -104,6 +105,8 @@ def load():
     _sig(lib, "gss_check_pass_host", c_int, vp, vp, c_i64, c_int, vp, vp, vp, c_i64, vp)
     _sig(lib, "gss_check_passes_host", c_int, vp, c_int, vp, c_i64, c_int, vp, vp, vp, vp, vp)
     _sig(lib, "gss_check_passes_host_packed", c_int, vp, c_int, vp, c_i64, c_int, vp, vp, vp, vp, vp)
+    _sig(lib, "gss_check_passes_host_cells", c_int, vp, c_int, vp, c_i64, c_int, vp, vp, vp, vp, vp)
+    _sig(lib, "gss_probe_gather", c_int, c_int, ctypes.c_uint64, c_int, c_int, vp, vp)
     _sig(lib, "gss_db_positions", c_int, vp, vp, c_i64, vp)
     _sig(lib, "gss_engine_set_length_plan", c_int, vp, c_int, vp, vp)
     _sig(lib, "gss_order_params_default", None, vp)
@@ -489,23 +492,27 @@ def bench_plant(lits_ptr, offsets_ptr, n_clauses, rate_ptr, state_ptr, base_ptr,
                                _vp(stream) if stream else None))
 
 
-def passes_host(engine, states, start, solver_of_word=None, caps=None, packed=False):
-    """Pipelined passes through host buffers (gss_check_passes_host, or
-    gss_check_passes_host_packed for 12-byte records); returns one report
-    array per state."""
-    lib = engine.lib
+def passes_host(engine, states, start, solver_of_word=None, caps=None, packed=False, records=None):
+    """Pipelined passes through host buffers; returns one report array per
+    state. records: "full" (gss_check_passes_host, REPORT_DTYPE), "packed"
+    (gss_check_passes_host_packed, 12-byte records) or "cells"
+    (gss_check_passes_host_cells, 8-byte {clause * n_words + word, mask});
+    packed=True is records="packed"."""
+    records = records or ("packed" if packed else "full")
+    dtype, fn = {"full": (REPORT_DTYPE, engine.lib.gss_check_passes_host),
+                 "packed": (PACKED_REPORT_DTYPE, engine.lib.gss_check_passes_host_packed),
+                 "cells": (CELL_REPORT_DTYPE, engine.lib.gss_check_passes_host_cells)}[records]
     n = len(states)
     states = [np.ascontiguousarray(s, dtype=np.uint32) for s in states]
     start = np.ascontiguousarray(start, dtype=np.uint32)
     sow = None if solver_of_word is None else np.ascontiguousarray(solver_of_word, dtype=np.int32)
     caps = caps or [1 << 20] * n
     while True:
-        outs = [np.zeros(max(int(c), 1), dtype=PACKED_REPORT_DTYPE if packed else REPORT_DTYPE) for c in caps]
+        outs = [np.zeros(max(int(c), 1), dtype=dtype) for c in caps]
         sp = (ctypes.c_void_p * n)(*[s.ctypes.data for s in states])
         op = (ctypes.c_void_p * n)(*[o.ctypes.data for o in outs])
         cp = np.ascontiguousarray(caps, dtype=np.int64)
         nr = np.zeros(n, dtype=np.int64)
-        fn = lib.gss_check_passes_host_packed if packed else lib.gss_check_passes_host
         rc = fn(engine.h, n, sp, states[0].shape[0], states[0].shape[1], _ptr(start), _ptr(sow), op, _ptr(cp),
                 _ptr(nr))
         if rc == GSS_ERR_OVERFLOW:
@@ -513,6 +520,25 @@ def passes_host(engine, states, start, solver_of_word=None, caps=None, packed=Fa
             continue
         _check(rc)
         return [o[:k] for o, k in zip(outs, nr)]
+
+
+def probe_gather(buffer_bytes, depth=2, blocks_per_sm=8, device=0):
+    """Random 256-byte row gathers over a device buffer (gss_probe_gather):
+    returns (rows per second, ms per launch)."""
+    lib = load()
+    rps = ctypes.c_double()
+    ms = ctypes.c_double()
+    _check(lib.gss_probe_gather(device, int(buffer_bytes), depth, blocks_per_sm, ctypes.byref(rps), ctypes.byref(ms)))
+    return rps.value, ms.value
+
+
+def cells_to_reports(cells, n_words):
+    """8-byte cell records -> PACKED_REPORT_DTYPE {clause, word, mask}."""
+    out = np.zeros(len(cells), dtype=PACKED_REPORT_DTYPE)
+    out["clause"] = cells["cell"] // np.uint32(n_words)
+    out["word"] = cells["cell"] % np.uint32(n_words)
+    out["mask"] = cells["mask"]
+    return out
 
 
 def sort_reports(rep):

@@ -167,9 +167,10 @@ struct GatherArgs {
 };
 int gather_clauses(const GatherArgs &a, cudaStream_t stream, int sm_count);
 // Packs report partitions (n_parts x cap records, counts[p] valid in
-// partition p, device) into contiguous 12-byte {clause, word, mask} records.
+// partition p, device) into contiguous 12-byte {clause, word, mask} records,
+// or, with cell_words > 0, 8-byte {clause * cell_words + word, mask} records.
 int launch_pack_reports(const gss_report *parts, const uint32_t *counts, uint32_t n_parts, uint32_t cap,
-                        uint32_t *packed, cudaStream_t stream, int sm_count);
+                        uint32_t cell_words, uint32_t *packed, cudaStream_t stream, int sm_count);
 // Synchronizes `stream`; returns the live clause and literal counts.
 int compact_by_id(const CompactArgs &a, cudaStream_t stream, int sm_count, uint32_t *n_out, int64_t *lits_out);
 

@@ -191,11 +191,13 @@ __global__ void pad_kernel(int32_t *new_lits, int64_t n_lits) {
     if (threadIdx.x < kClausePad) new_lits[n_lits + threadIdx.x] = 0;
 }
 
-// Packs the records of n_parts report partitions into one contiguous array of
-// 12-byte records {clause, word, mask}: partition p's first counts[p] records
-// (at most cap) go after the records of partitions 0..p-1.
+// Packs the records of n_parts report partitions into one contiguous array:
+// partition p's first counts[p] records (at most cap) go after the records of
+// partitions 0..p-1. cell_words == 0: 12-byte records {clause, word, mask};
+// otherwise 8-byte records {clause * cell_words + word, mask}.
 __global__ void pack_reports_kernel(const gss_report *__restrict__ parts, const uint32_t *__restrict__ counts,
-                                    uint32_t n_parts, uint32_t cap, uint32_t *__restrict__ packed) {
+                                    uint32_t n_parts, uint32_t cap, uint32_t cell_words,
+                                    uint32_t *__restrict__ packed) {
     const uint64_t total = (uint64_t) n_parts * cap;
     for (uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x; i < total;
          i += (uint64_t) gridDim.x * blockDim.x) {
@@ -204,22 +206,26 @@ __global__ void pack_reports_kernel(const gss_report *__restrict__ parts, const 
         uint64_t base = 0;
         for (uint32_t q = 0; q < p; q++) base += min(__ldg(counts + q), cap);
         const gss_report r = parts[i];
-        uint32_t *o = packed + 3 * (base + k);
-        o[0] = r.clause;
-        o[1] = r.word;
-        o[2] = r.mask;
+        if (cell_words) {
+            reinterpret_cast<uint2 *>(packed)[base + k] = make_uint2(r.clause * cell_words + r.word, r.mask);
+        } else {
+            uint32_t *o = packed + 3 * (base + k);
+            o[0] = r.clause;
+            o[1] = r.word;
+            o[2] = r.mask;
+        }
     }
 }
 
 }  // namespace
 
 int launch_pack_reports(const gss_report *parts, const uint32_t *counts, uint32_t n_parts, uint32_t cap,
-                        uint32_t *packed, cudaStream_t stream, int sm_count) {
+                        uint32_t cell_words, uint32_t *packed, cudaStream_t stream, int sm_count) {
     const uint64_t total = (uint64_t) n_parts * cap;
     if (total == 0) return GSS_OK;
     uint64_t blocks = (total + 255) / 256;
     if (blocks > (uint64_t) sm_count * 16) blocks = (uint64_t) sm_count * 16;
-    pack_reports_kernel<<<(unsigned) blocks, 256, 0, stream>>>(parts, counts, n_parts, cap, packed);
+    pack_reports_kernel<<<(unsigned) blocks, 256, 0, stream>>>(parts, counts, n_parts, cap, cell_words, packed);
     GSS_CUDA_TRY(cudaGetLastError());
     return GSS_OK;
 }

@@ -413,7 +413,10 @@ void mirror_append(gss_engine *eng, const int32_t *lits, const int64_t *offsets,
         length_order(offsets, n, order);
     }
     if (eng->h_off.empty()) eng->h_off.push_back(0);
-    eng->h_lits.reserve(eng->h_lits.size() + (size_t) (n > 0 ? offsets[n] - offsets[0] : 0));
+    // room by doubling: an exact reserve per append would copy the whole
+    // host database at every append of a clause stream
+    const size_t want = eng->h_lits.size() + (size_t) (n > 0 ? offsets[n] - offsets[0] : 0);
+    if (want > eng->h_lits.capacity()) eng->h_lits.reserve(std::max(want, 2 * eng->h_lits.capacity()));
     for (int64_t k = 0; k < n; k++) {
         const int64_t c = order[k];
         const int64_t len = offsets[c + 1] - offsets[c];
@@ -1067,11 +1070,20 @@ int gss_check_pass_host(gss_engine *eng, const uint32_t *state, int64_t n_vars, 
 
 namespace {
 
+// Record formats of passes through host buffers.
+enum HostRecords { kRecordsFull = 0, kRecordsPacked = 1, kRecordsCells = 2 };
+
 // Passes through host buffers; outs[i] receives gss_report records, or
-// 12-byte {clause, word, mask} records packed on the device when `packed`.
+// records packed on the device: 12-byte {clause, word, mask} (kRecordsPacked)
+// or 8-byte {clause * n_words + word, mask} (kRecordsCells).
 int passes_host(gss_engine *eng, int n_passes, const uint32_t *const *states, int64_t n_vars, int n_words,
                 const uint32_t *start, const int32_t *solver_of_word, void *const *outs, const int64_t *caps,
-                int64_t *n_reports, bool packed) {
+                int64_t *n_reports, int format) {
+    const bool packed = format != kRecordsFull;
+    const uint32_t rec_words = format == kRecordsCells ? 2u : 3u;  // 32-bit words per packed record
+    if (format == kRecordsCells && eng && n_words > 0 && (uint64_t) eng->next_id * (uint64_t) n_words > 0xFFFFFFFFull)
+        return set_error(GSS_ERR_INVALID, "cell records need (largest clause id + 1) x words <= 2^32 (%u ids x %d words)",
+                         eng->next_id, n_words);
     // Passes i = 0..n-1 over three streams: the state of pass i+1 goes
     // host->device (h2d stream) and the reports of pass i-1 come back (d2h
     // stream) while pass i runs (engine stream). Three buffer slots: state b
@@ -1112,7 +1124,7 @@ int passes_host(gss_engine *eng, int n_passes, const uint32_t *const *states, in
     GSS_TRY(eng->counts3.reserve(sizeof(uint32_t) * eng->n_parts));
     auto reserve_packed = [&]() -> int {
         for (int b = 0; b < NB && packed; b++)
-            GSS_TRY(eng->packed[b].reserve((size_t) eng->cap_per_part * eng->n_parts * 3 * sizeof(uint32_t)));
+            GSS_TRY(eng->packed[b].reserve((size_t) eng->cap_per_part * eng->n_parts * rec_words * sizeof(uint32_t)));
         return GSS_OK;
     };
     GSS_TRY(reserve_packed());
@@ -1120,7 +1132,8 @@ int passes_host(gss_engine *eng, int n_passes, const uint32_t *const *states, in
     auto pack = [&](int b, const DevBuf &rep, const DevBuf &cnt) -> int {
         if (!packed) return GSS_OK;
         return launch_pack_reports((const gss_report *) rep.ptr, (const uint32_t *) cnt.ptr, eng->n_parts,
-                                   eng->cap_per_part, (uint32_t *) eng->packed[b].ptr, eng->stream, eng->sm_count);
+                                   eng->cap_per_part, format == kRecordsCells ? (uint32_t) n_words : 0u,
+                                   (uint32_t *) eng->packed[b].ptr, eng->stream, eng->sm_count);
     };
     GSS_TRY(eng->h_counts2.reserve(sizeof(uint32_t) * (eng->n_parts + 1)));
     GSS_TRY(eng->h_counts3.reserve(sizeof(uint32_t) * (eng->n_parts + 1)));
@@ -1176,8 +1189,9 @@ int passes_host(gss_engine *eng, int n_passes, const uint32_t *const *states, in
                              (long long) total);
         if (packed) {
             if (total)
-                GSS_CUDA_TRY(cudaMemcpyAsync(outs[j], eng->packed[b].ptr, (size_t) total * 3 * sizeof(uint32_t),
-                                             cudaMemcpyDeviceToHost, eng->d2h));
+                GSS_CUDA_TRY(cudaMemcpyAsync(outs[j], eng->packed[b].ptr,
+                                             (size_t) total * rec_words * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                                             eng->d2h));
         } else {
             int64_t pos = 0;
             for (uint32_t p = 0; p < eng->n_parts; p++) {
@@ -1237,14 +1251,21 @@ int gss_check_passes_host(gss_engine *eng, int n_passes, const uint32_t *const *
                           int n_words, const uint32_t *start, const int32_t *solver_of_word, gss_report *const *outs,
                           const int64_t *caps, int64_t *n_reports) {
     return passes_host(eng, n_passes, states, n_vars, n_words, start, solver_of_word, (void *const *) outs, caps,
-                       n_reports, false);
+                       n_reports, kRecordsFull);
 }
 
 int gss_check_passes_host_packed(gss_engine *eng, int n_passes, const uint32_t *const *states, int64_t n_vars,
                                  int n_words, const uint32_t *start, const int32_t *solver_of_word,
                                  gss_report_packed *const *outs, const int64_t *caps, int64_t *n_reports) {
     return passes_host(eng, n_passes, states, n_vars, n_words, start, solver_of_word, (void *const *) outs, caps,
-                       n_reports, true);
+                       n_reports, kRecordsPacked);
+}
+
+int gss_check_passes_host_cells(gss_engine *eng, int n_passes, const uint32_t *const *states, int64_t n_vars,
+                                int n_words, const uint32_t *start, const int32_t *solver_of_word,
+                                gss_report_cell *const *outs, const int64_t *caps, int64_t *n_reports) {
+    return passes_host(eng, n_passes, states, n_vars, n_words, start, solver_of_word, (void *const *) outs, caps,
+                       n_reports, kRecordsCells);
 }
 
 }  // extern "C"

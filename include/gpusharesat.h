@@ -243,6 +243,29 @@ typedef struct gss_report_packed {
 int gss_check_passes_host_packed(gss_engine *eng, int n_passes, const uint32_t *const *states, int64_t n_vars,
                                  int n_words, const uint32_t *start, const int32_t *solver_of_word,
                                  gss_report_packed *const *outs, const int64_t *caps, int64_t *n_reports);
+/* The same passes with 8-byte records {cell, mask}, where cell = clause *
+ * n_words + word (so clause = cell / n_words, word = cell % n_words): a third
+ * less than the 12-byte records over the host link. Needs (largest clause id
+ * + 1) x n_words <= 2^32, else GSS_ERR_INVALID. No counterpart in the
+ * reference. */
+typedef struct gss_report_cell {
+    uint32_t cell;
+    uint32_t mask;
+} gss_report_cell;
+int gss_check_passes_host_cells(gss_engine *eng, int n_passes, const uint32_t *const *states, int64_t n_vars,
+                                int n_words, const uint32_t *start, const int32_t *solver_of_word,
+                                gss_report_cell *const *outs, const int64_t *caps, int64_t *n_reports);
+
+/* ---- measurement probe ----
+ * No counterpart in the reference. Random 256-byte row gathers, the access
+ * pattern of the check kernels (one state row per literal visit), without the
+ * rule: groups of 8 lanes load one random row each (32 bytes a lane), `depth`
+ * rows in flight per group (1, 2 or 4), blocks_per_sm blocks of 256 threads
+ * per SM, over a fresh device buffer of buffer_bytes. Returns the rows
+ * delivered per second and the time of one launch. Allocates and frees the
+ * buffer itself; synchronous. */
+int gss_probe_gather(int device, uint64_t buffer_bytes, int depth, int blocks_per_sm, double *rows_per_s,
+                     double *ms_per_launch);
 
 /* ---- allocation-free check pass ----
  * No counterpart in the reference. For callers that cannot allocate device

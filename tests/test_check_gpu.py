@@ -151,11 +151,12 @@ def test_pass_through_host_buffers(engine):
     _assert_same(rep, ref, wl)
 
 
-@pytest.mark.parametrize("packed", [False, True])
-def test_pipelined_passes_through_host_buffers(engine, packed):
+@pytest.mark.parametrize("records", ["full", "packed", "cells"])
+def test_pipelined_passes_through_host_buffers(engine, records):
     """Several passes with different states, pipelined over three streams, each
     equal to the oracle; small output capacities force the overflow path.
-    Packed: the 12-byte records packed on the device."""
+    packed: the 12-byte records packed on the device; cells: the 8-byte
+    {clause * n_words + word, mask} records."""
     import gpusharesat_gb300 as g
     rng = np.random.default_rng(17)
     base = W.make_scale(seed=17, n_vars=2 ** 12, n_clauses=30000, n_solvers=32)
@@ -163,11 +164,26 @@ def test_pipelined_passes_through_host_buffers(engine, packed):
     engine.set_db(base.lits, base.offsets)
     for caps in (None, [100] * 5):
         engine.set_capacity(0 if caps is None else 50)
-        got = g.passes_host(engine, states, base.start, base.solver_of_word, caps=caps, packed=packed)
+        got = g.passes_host(engine, states, base.start, base.solver_of_word, caps=caps, records=records)
         for st, rep in zip(states, got):
+            if records == "cells":
+                rep = g.cells_to_reports(rep, 32)
             ref = oracle.check(base.lits, base.offsets, st, base.start)
             _assert_same(g.sort_reports(rep), ref)
     engine.set_capacity(0)
+
+
+def test_cell_records_refuse_ids_past_32_bits(engine):
+    """Cell records need (largest id + 1) x words <= 2^32: a clause id of 2^22
+    over 1024 words is refused, not wrapped."""
+    import gpusharesat_gb300 as g
+    engine.set_db(np.array([2, 4], np.int32), np.array([0, 2], np.int64))
+    engine.append_db(np.array([2, 6], np.int32), np.array([0, 2], np.int64), np.array([1 << 22], np.uint32))
+    n_words = 1024
+    state = np.zeros((8, n_words, 2), np.uint32)
+    with pytest.raises(g.GssError):
+        g.passes_host(engine, [state], np.full(n_words, 0xFFFFFFFF, np.uint32), np.arange(n_words, dtype=np.int32),
+                      records="cells")
 
 
 import kat  # noqa: E402
