@@ -7,6 +7,7 @@ baseline, and prints one JSON line per pass plus a summary line:
     python -m gpusharesat_gb300.bench_configs batching [--clauses 8000000 --passes 6]
     python -m gpusharesat_gb300.bench_configs serving [--rates 5e4 1e5 2e5 --budget 16000000]
     python -m gpusharesat_gb300.bench_configs learned [--clauses 4000000 --passes 3000 --retrain 1000]
+    python -m gpusharesat_gb300.bench_configs gather [--passes 20]
 
 batching: 8e6 clauses (lengths 1 + Zipf(1.2), at most 256), 48 solvers sending
     uneven batches of 4..64 assignments per pass (two 32-slot words each), 5%
@@ -47,6 +48,16 @@ learned: 2^21 variables; 4e6 clauses at the start (lengths 1 + Zipf(1.2),
     first 10%, the delivery latency of report bits (from the launch call to
     the moment the host has them), checks/s of both forms, and that each
     compared pass reports what the plain scan reports.
+
+gather: the bound of the check kernels. Random 256-byte row gathers
+    (gss_probe_gather: 8 lanes x 32 bytes a row, 2 rows in flight per group,
+    8 blocks of 256 threads per SM) over buffers of 32 MB to 1 GB, the host
+    link's pinned copy rates (each direction, then both at once), then the
+    default check kernel on the at-scale workload (4e6 clauses x 1024
+    assignments) with 2^17 variables (a 32 MB state, resident in L2) and
+    with 2^20 variables (256 MB, the benchmark's): the kernel time with the
+    state in L2 is the floor its instruction issue and latency set; the
+    difference at 2^20 is what the misses to DRAM cost.
 """
 import argparse
 import json
@@ -322,13 +333,15 @@ def learned(args):
         eng.wait()
         ta = time.perf_counter()
         eng.launch()
+        tl = time.perf_counter()
         head = eng.wait_head(cap=bufs[0].shape[0], out=bufs[0])
         tb = time.perf_counter()
         tail = eng.copy_tail(cap=bufs[1].shape[0], out=bufs[1])
         tc = time.perf_counter()
         st = eng.order_stats()
         head_bits = _bits(head)
-        row = {"pass": p, "head_bits": head_bits, "bits": head_bits + _bits(tail), "head_ms": (tb - ta) * 1e3,
+        row = {"pass": p, "head_bits": head_bits, "bits": head_bits + _bits(tail), "launch_call_ms": (tl - ta) * 1e3,
+               "head_ms": (tb - ta) * 1e3,
                "all_ms": (tc - ta) * 1e3, "score_dev_ms": st["score_ms"], "head_dev_ms": st["head_ms"],
                "tail_dev_ms": st["tail_ms"], "trainings": st["trainings"]}
         if p % args.compare_every == 0:
@@ -341,8 +354,10 @@ def learned(args):
             eng.kernel_time()
             td = time.perf_counter()
             eng.launch()
+            tl2 = time.perf_counter()
             plain = eng.reports(out=bufs[2])
             te = time.perf_counter()
+            row["plain_launch_call_ms"] = (tl2 - td) * 1e3
             row["plain_all_ms"] = (te - td) * 1e3
             row["plain_dev_ms"] = eng.kernel_time()[0]
             eng.set_timing(False)
@@ -376,6 +391,14 @@ def learned(args):
         lw += [r["head_bits"], r["bits"] - r["head_bits"]]
         pv.append(r["plain_all_ms"])
         pw.append(r["bits"])
+    # the same on the device clock: head bits when the head launch ends, the
+    # rest when the tail ends (the scoring ran during the previous pass),
+    # against the plain launch's end
+    dv, dw, dp = [], [], []
+    for r in cmp_rows:
+        dv += [r["head_dev_ms"], r["head_dev_ms"] + r["tail_dev_ms"]]
+        dw += [r["head_bits"], r["bits"] - r["head_bits"]]
+        dp.append(r["plain_dev_ms"])
     checks_ordered = [(nxt - lo) * 32 * n_words / (r["all_ms"] / 1e3) for r in cmp_rows]
     checks_plain = [(nxt - lo) * 32 * n_words / (r["plain_all_ms"] / 1e3) for r in cmp_rows]
     summary = {"config": "learned", "passes": P, "trained_passes": len(trained), "compared_passes": len(cmp_rows),
@@ -387,6 +410,13 @@ def learned(args):
                "latency_p50_ms_plain": _weighted_quantile(pv, pw, 0.5) if cmp_rows else None,
                "latency_p99_ms_learned": _weighted_quantile(lv, lw, 0.99) if cmp_rows else None,
                "latency_p99_ms_plain": _weighted_quantile(pv, pw, 0.99) if cmp_rows else None,
+               "device_latency_p50_ms_learned": _weighted_quantile(dv, dw, 0.5) if cmp_rows else None,
+               "device_latency_p99_ms_learned": _weighted_quantile(dv, dw, 0.99) if cmp_rows else None,
+               "device_latency_p50_ms_plain": _weighted_quantile(dp, pw, 0.5) if cmp_rows else None,
+               "device_latency_p99_ms_plain": _weighted_quantile(dp, pw, 0.99) if cmp_rows else None,
+               "launch_call_ms_learned": float(np.mean([r["launch_call_ms"] for r in cmp_rows])) if cmp_rows else None,
+               "launch_call_ms_plain": float(np.mean([r["plain_launch_call_ms"] for r in cmp_rows]))
+               if cmp_rows else None,
                "pass_ms_learned": float(np.mean([r["all_ms"] for r in cmp_rows])) if cmp_rows else None,
                "pass_ms_plain": float(np.mean([r["plain_all_ms"] for r in cmp_rows])) if cmp_rows else None,
                "score_dev_ms": float(np.mean([r["score_dev_ms"] for r in trained])) if trained else None,
@@ -403,9 +433,72 @@ def learned(args):
     return summary
 
 
+def _host_link(mb=256, reps=5):
+    """Pinned host <-> device copy rates: one direction at a time, then both
+    at once on two streams (best of `reps`, wall clock around synchronize)."""
+    import torch
+    n = mb << 20
+    dev = torch.device("cuda:0")
+    h_in = torch.ones(n, dtype=torch.uint8).pin_memory()
+    h_out = torch.empty(n, dtype=torch.uint8).pin_memory()
+    d_in = torch.empty(n, dtype=torch.uint8, device=dev)
+    d_out = torch.ones(n, dtype=torch.uint8, device=dev)
+    s_up, s_down = torch.cuda.Stream(), torch.cuda.Stream()
+    rows = []
+    for name, up, down in (("host->device", True, False), ("device->host", False, True), ("both", True, True)):
+        best = float("inf")
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            if up:
+                with torch.cuda.stream(s_up):
+                    d_in.copy_(h_in, non_blocking=True)
+            if down:
+                with torch.cuda.stream(s_down):
+                    h_out.copy_(d_out, non_blocking=True)
+            torch.cuda.synchronize()
+            best = min(best, time.perf_counter() - t0)
+        moved = n * (int(up) + int(down))
+        row = {"host_link": name, "mb_each_way": mb, "ms": best * 1e3, "gb_per_s": moved / best / 1e9}
+        rows.append(row)
+        print(json.dumps(row), flush=True)
+    return rows
+
+
+def gather(args):
+    """Row-gather probe over several working sets, then the default check
+    kernel with its state in L2 and in DRAM (see the module docstring)."""
+    rows = []
+    for mb in (32, 64, 96, 128, 192, 256, 1024):
+        rps, ms = g.probe_gather(mb << 20, depth=2, blocks_per_sm=8)
+        row = {"probe": "random 256-byte rows", "buffer_mb": mb, "rows_per_s": rps, "ms_per_launch": ms,
+               "tb_per_s": rps * 256 / 1e12}
+        rows.append(row)
+        print(json.dumps(row), flush=True)
+    rows += _host_link()
+    for vl in (17, 20):
+        wl = W.make_scale(seed=1, n_vars=2 ** vl)
+        eng = g.Engine(0)
+        try:
+            eng.set_db(wl.lits, wl.offsets)
+            eng.set_state(wl.state, wl.start, wl.solver_of_word)
+            n = len(eng.check())
+            for _ in range(5):
+                eng.launch()
+            ms = _timed(eng, lambda: [eng.launch() for _ in range(args.passes)]) / args.passes
+        finally:
+            eng.close()
+        row = {"kernel": "default check kernel", "variables": 2 ** vl, "state_mb": (2 ** vl) * 256 / 2 ** 20,
+               "clauses": wl.n_clauses, "slots": 1024, "reports": n, "ms_per_pass": ms,
+               "literal_visits_note": "about 8.4 state-row gathers per clause"}
+        rows.append(row)
+        print(json.dumps(row), flush=True)
+    return rows
+
+
 def main(argv=None):
     p = argparse.ArgumentParser()
-    p.add_argument("config", choices=["batching", "serving", "learned"])
+    p.add_argument("config", choices=["batching", "serving", "learned", "gather"])
     p.add_argument("--clauses", type=int, default=8_000_000)
     p.add_argument("--passes", type=int, default=6)
     p.add_argument("--rates", type=float, nargs="+", default=[5e4, 1e5, 2e5])
@@ -431,6 +524,10 @@ def main(argv=None):
         serving(args)
     elif args.config == "learned":
         learned(args)
+    elif args.config == "gather":
+        if "--passes" not in (argv or sys.argv):
+            args.passes = 20
+        gather(args)
 
 
 if __name__ == "__main__":
