@@ -418,7 +418,8 @@ class OrderParams(ctypes.Structure):
     """gss_order_params."""
     _fields_ = [("head_fraction", ctypes.c_double), ("retrain_interval", ctypes.c_int), ("train_epochs", ctypes.c_int),
                 ("batch", ctypes.c_int), ("learning_rate", ctypes.c_float), ("log_capacity", ctypes.c_int64),
-                ("log_rate", ctypes.c_double), ("seed", ctypes.c_uint64), ("overlap", ctypes.c_int)]
+                ("log_rate", ctypes.c_double), ("seed", ctypes.c_uint64), ("overlap", ctypes.c_int),
+                ("rescore_interval", ctypes.c_int)]
 
 
 class OrderStats(ctypes.Structure):

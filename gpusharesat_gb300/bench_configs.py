@@ -46,8 +46,9 @@ learned: 2^21 variables; 4e6 clauses at the start (lengths 1 + Zipf(1.2),
     kernel, no order) checks the same state. Reports the share of report
     bits in the first 10% of the learned scan against the plain order's
     first 10%, the delivery latency of report bits (from the launch call to
-    the moment the host has them), checks/s of both forms, and that each
-    compared pass reports what the plain scan reports.
+    the moment the host has them, and on the device clock), sustained
+    checks/s of both forms over back-to-back passes, and that each compared
+    pass reports what the plain scan reports.
 
 gather: the bound of the check kernels. Random 256-byte row gathers
     (gss_probe_gather: 8 lanes x 32 bytes a row, 2 rows in flight per group,
@@ -307,7 +308,7 @@ def learned(args):
     eng.set_variant(*composed)
     eng.set_db(lits[:offsets[n0]], offsets[:n0 + 1])
     eng.order_enable(head_fraction=args.head_fraction, retrain_interval=args.retrain, train_epochs=2, seed=4,
-                     overlap=args.overlap)
+                     overlap=args.overlap, rescore_interval=args.rescore)
     eng.set_lbd(np.arange(n0, dtype=np.uint32), d["lbd"][:n0])
     # room for the planted reports of a pass (about 0.75 records per clause at 64 words)
     eng.set_capacity(max(1 << 22, 2 * n0))
@@ -378,6 +379,32 @@ def learned(args):
         torch.cuda.synchronize()
         if p % 100 == 0:
             print(json.dumps(row), flush=True)
+    # sustained passes, back to back on the last pass's state, with no report
+    # handling on the host: the ordered form (scoring of the next pass on its
+    # own stream, head and tail launches, history) against the plain single
+    # launch; wall clock over K passes, each waited for before the next
+    thr = {}
+    if args.throughput_passes > 0:
+        K = args.throughput_passes
+        live = nxt - lo
+        for name in ("learned", "plain", "persistent", "learned"):
+            learned_form = name == "learned"
+            eng.order_set_active(learned_form)
+            eng.set_variant(*(plain_variant if name == "plain" else composed))
+            for _ in range(3):
+                eng.launch()
+                eng.wait()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(K):
+                eng.launch()
+                eng.wait()
+            torch.cuda.synchronize()
+            dt = (time.perf_counter() - t0) / K
+            thr[name] = {"ms_per_pass": dt * 1e3, "checks_per_s": live * 32 * n_words / dt}
+        eng.set_variant(*composed)
+        eng.order_set_active(True)
+        print(json.dumps({"throughput_passes": K, **{k: v for k, v in thr.items()}}), flush=True)
     trained = [r for r in rows if r["trainings"] >= 1 and r["bits"]]
     cmp_rows = [r for r in trained if "plain_all_ms" in r]
     cmp_bits = max(1, np.sum([r["bits"] for r in cmp_rows]))
@@ -423,9 +450,14 @@ def learned(args):
                "device_ms_learned": float(np.mean([r["score_dev_ms"] + r["head_dev_ms"] + r["tail_dev_ms"]
                                                    for r in cmp_rows])) if cmp_rows else None,
                "device_ms_plain": float(np.mean([r["plain_dev_ms"] for r in cmp_rows])) if cmp_rows else None,
-               "overlap": args.overlap,
+               "overlap": args.overlap, "rescore_interval": args.rescore,
                "checks_per_s_learned": float(np.mean(checks_ordered)) if cmp_rows else None,
                "checks_per_s_plain": float(np.mean(checks_plain)) if cmp_rows else None,
+               "sustained_ms_per_pass_learned": thr["learned"]["ms_per_pass"] if thr else None,
+               "sustained_ms_per_pass_plain": thr["plain"]["ms_per_pass"] if thr else None,
+               "sustained_checks_per_s_learned": thr["learned"]["checks_per_s"] if thr else None,
+               "sustained_checks_per_s_plain": thr["plain"]["checks_per_s"] if thr else None,
+               "sustained_ms_per_pass_persistent_no_order": thr["persistent"]["ms_per_pass"] if thr else None,
                "same_reports_every_compared_pass": all(r["same_reports"] for r in rows if "same_reports" in r),
                "trainings": rows[-1]["trainings"] if rows else 0}
     print(json.dumps(summary), flush=True)
@@ -510,6 +542,10 @@ def main(argv=None):
     p.add_argument("--head-fraction", type=float, default=0.25)
     p.add_argument("--compare-every", type=int, default=5)
     p.add_argument("--overlap", type=int, default=1)
+    p.add_argument("--rescore", type=int, default=1,
+                   help="learned: passes per scoring and sort (the passes between keep the last order)")
+    p.add_argument("--throughput-passes", type=int, default=50,
+                   help="learned: back-to-back passes of each form for the sustained checks/s (0: skip)")
     p.add_argument("--compare-plain", type=int, default=1,
                    help="serving: also run each rate with the plain single-launch scan")
     args = p.parse_args(argv)

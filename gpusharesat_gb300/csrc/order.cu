@@ -4,13 +4,18 @@
 // checked each pass: the report set is the plain scan's.
 //
 // Per pass (score_pass):
-//   1-2. score_kernel, a lane per clause position (a warp per 32): folds the
-//      clause's report count of pass q-2 into its 8-pass history (a byte per
-//      pass; the first time an id is seen, its birth), logs a sample of
-//      (features, reported) rows for training, computes the features; the
-//      warp runs the MLP on tensor cores (mma.sync m16n8k16, BF16 operands,
-//      FP32 accumulation) over its 32 clauses as two m16 tiles, and each lane
-//      writes its clause's score bucket
+//   1. the history step: birth_kernel (records of the ids first seen),
+//      log_kernel (a hashed sample of (features, reported) rows of pass q-2
+//      for training), fold_kernel (a sweep over the ids in id order: pass
+//      q-2's report counts folded into the 8-pass histories of the clauses it
+//      reported; the others are not written, their histories read as shifted
+//      by the passes since their last report)
+//   Every rescore_interval passes (or when the layout changed), the scan
+//   permutation is rebuilt; the passes between reuse it:
+//   2. score_kernel, a lane per clause position (a warp per 32): computes
+//      the features; the warp runs the MLP on tensor cores (mma.sync
+//      m16n8k16, BF16 operands, FP32 accumulation) over its 32 clauses as two
+//      m16 tiles, and each lane writes its clause's score bucket
 //   3. bucket_hist_kernel, bucket_scan_kernel, head_key_kernel, then a
 //      stable one-digit radix sort of positions (bucket_hist, bucket_scan,
 //      bucket_base, bucket_scatter) by key: the score bucket for the clauses
@@ -110,10 +115,13 @@ __host__ __device__ __forceinline__ void clause_features(uint32_t len, uint32_t 
     x[11] = rate < 1.0f ? rate : 1.0f;
 }
 
-// Per-id history (device), one 32-byte record per clause id: read with one
-// sector gather and written back with one store per pass.
+// Per-id history (device), one 32-byte record per clause id. The history is
+// kept lazily: a pass touches only the records of the clauses it reported
+// (history_kernel lists them, fold_kernel folds them in), and `hist` holds the
+// counts as of the pass of the last report; readers shift it to the pass they
+// need (hist_at), the passes in between having had no report.
 struct alignas(32) ClauseRecord {  // field order is read as two uint4 by score_kernel
-    uint64_t hist;   // byte k = slot reports in pass (now - 1 - k), saturated at 255
+    uint64_t hist;   // byte k = slot reports in pass (last - k), saturated at 255
     uint32_t total;  // slot reports over the clause's life
     int32_t last;    // pass of the last report, -1 never
     int32_t birth;   // the `now` of the first scoring that saw the clause
@@ -124,9 +132,18 @@ struct alignas(32) ClauseRecord {  // field order is read as two uint4 by score_
 };
 static_assert(sizeof(ClauseRecord) == 32, "one sector per clause");
 
-// Scoring for pass q folds the counts of pass q-2 (slot q & 1) into the
-// history: pass q-1 may still be running when pass q is scored. Features
-// are then those of a prediction for the pass after `now` = q-1.
+// The history word with byte 0 = pass t, from a record whose byte 0 is pass
+// `last` (no report after it): all zero for a clause that never reported.
+__host__ __device__ __forceinline__ uint64_t hist_at(uint64_t hist, int32_t last, int32_t t) {
+    if (last < 0) return 0;
+    const int32_t d = t - last;
+    return d >= 8 ? 0ull : d <= 0 ? hist : hist << (8 * d);
+}
+
+// The step before the scoring of pass q folds the counts of pass q-2 (slot
+// q & 1) into the history: pass q-1 may still be running when pass q is
+// scored. Features are then those of a prediction for the pass after
+// `now` = q-1, with the history through pass q-2.
 struct HistoryArgs {
     ClauseRecord *rec;
     uint32_t n_ids;
@@ -510,7 +527,15 @@ struct OrderState {
     DevBuf rec;                                 // ClauseRecord per clause id
     DevBuf lbd_pairs;                           // staging of gss_db_set_lbd
     DevBuf bucket, offs, totals, key_of;        // per position; per (bucket, sort tile); per bucket (x2)
-    DevBuf perm[2];                             // scan permutation of passes with even / odd numbers
+    DevBuf perm[2];                             // scan permutations: the current one and the next one
+    // the scan permutation in force (rescored every rescore_interval passes):
+    // its buffer, the positions it covers and the layout it was built for;
+    // inflight_buf is the buffer of the pass in flight, which a rescoring
+    // must leave alone
+    bool perm_valid = false;
+    int perm_buf = 0, inflight_buf = 0;
+    uint32_t perm_n = 0;
+    uint64_t perm_layout = 0;
     // the order of the next pass, computed on score_stream while the tail of
     // the current pass runs (pre_*: what it was computed for)
     cudaStream_t score_stream = nullptr;
@@ -519,6 +544,7 @@ struct OrderState {
     int64_t pre_pass = -1;
     int64_t folded_pass = -1;  // the last pass q whose scoring folded pass q-2's counts
     uint32_t pre_n = 0;
+    int pre_buf = 0;
     uint64_t pre_layout = 0;
     DevBuf log_x, log_y, log_count;
     PinnedBuf h_head_counts, h_log_count;
@@ -551,13 +577,11 @@ struct LogArgs {
     uint64_t seed;
 };
 
-// One warp per 32 positions, a lane per position. For each live clause:
-// folds the report count of pass h.fold into its history (the first time an
-// id is seen: its birth), logs a sample of (features before the fold,
-// reported) rows, computes its features; then the lanes pass the features to
-// the MLP's fragment layout (two m16 tiles) and each lane writes its
-// clause's score bucket.
-__global__ void __launch_bounds__(kMlpThreads, 3) score_kernel(HistoryArgs h, LogArgs lg, const float *__restrict__ w,
+// One warp per 32 positions, a lane per position: the features of each live
+// clause from its history (through pass now - 1), then the lanes pass the
+// features to the MLP's fragment layout (two m16 tiles) and each lane writes
+// its clause's score bucket.
+__global__ void __launch_bounds__(kMlpThreads, 3) score_kernel(HistoryArgs h, const float *__restrict__ w,
                                                                const uint32_t *__restrict__ frag,
                                                                const int64_t *__restrict__ offsets,
                                                                const uint32_t *__restrict__ orig,
@@ -581,46 +605,11 @@ __global__ void __launch_bounds__(kMlpThreads, 3) score_kernel(HistoryArgs h, Lo
         if (live) {
             const uint32_t len = (uint32_t) (offsets[r + 1] - offsets[r]);
             // the record as two 16-byte words: {hist lo, hist hi, total, last}, {birth, cur0, lbd|pad, cur1}
-            ClauseRecord *rec = h.rec + id;
+            const ClauseRecord *rec = h.rec + id;
             const uint4 ra = reinterpret_cast<const uint4 *>(rec)[0], rb = reinterpret_cast<const uint4 *>(rec)[1];
-            const uint32_t lbd = rb.z & 0xFFFFu;
-            int32_t birth, last;
-            uint64_t hist;
-            uint32_t total;
-            const bool born = id >= h.known_ids;
-            if (born) {
-                birth = h.now, last = -1, hist = 0, total = 0;
-            } else {
-                birth = (int32_t) rb.x, last = (int32_t) ra.w, hist = ((uint64_t) ra.y << 32) | ra.x, total = ra.z;
-                const uint32_t c = h.fold >= 0 ? (h.slot ? rb.w : rb.y) : 0u;
-                // a training row: the features a prediction for pass `fold`
-                // would have used, and whether the clause reported in it
-                if (lg.cap && h.fold >= 0 && birth < h.fold && unit_hash(lg.seed, (uint64_t) h.fold, id) < lg.rate) {
-                    float xl[kF];
-                    clause_features(len, lbd, h.fold - birth, hist, total, last < 0 ? -1 : h.fold - last, xl);
-                    const unsigned long long slot = atomicAdd(lg.count, 1ull) % lg.cap;
-#pragma unroll
-                    for (int k = 0; k < kF; k++) lg.x[slot * kF + k] = xl[k];
-                    lg.y[slot] = c ? 1.0f : 0.0f;
-                }
-                if (h.fold >= 0) {
-                    hist = (hist << 8) | (uint64_t) (c < 255u ? c : 255u);
-                    total += c;
-                    if (c) last = h.fold;
-                }
-            }
-            // the history word and the folded slot; the other slot may be
-            // taking the counts of the pass in flight (history_kernel)
-            *reinterpret_cast<uint4 *>(rec) = make_uint4((uint32_t) hist, (uint32_t) (hist >> 32), total,
-                                                         (uint32_t) last);
-            if (born) rec->birth = birth;
-            if (h.fold >= 0) {
-                if (h.slot)
-                    rec->cur1 = 0;
-                else
-                    rec->cur0 = 0;
-            }
-            clause_features(len, lbd, h.now - birth, hist, total, last < 0 ? -1 : h.now - last, x);
+            const int32_t last = (int32_t) ra.w;
+            const uint64_t hist = hist_at(((uint64_t) ra.y << 32) | ra.x, last, h.now - 1);
+            clause_features(len, rb.z & 0xFFFFu, h.now - (int32_t) rb.x, hist, ra.z, last < 0 ? -1 : h.now - last, x);
         }
         // two m16 tiles: rows 0-15 and 16-31 of the warp's positions, their
         // features passed to the fragment layout through shared memory
@@ -651,6 +640,61 @@ __global__ void __launch_bounds__(kMlpThreads, 3) score_kernel(HistoryArgs h, Lo
         }
         if (r < n) bucket[r] = (uint8_t) (live ? bucket_of(logit) : (uint32_t) (kBuckets - 1));
         __syncwarp();  // wx is rewritten by the next tile
+    }
+}
+
+// Records of the ids first seen by the scoring step at `now` (ids in
+// [from, to)): born at `now`, no report yet. Their pass counters are kept
+// (a clause appended while a pass ran may already hold counts of it).
+__global__ void birth_kernel(ClauseRecord *__restrict__ rec, uint32_t from, uint32_t to, int32_t now) {
+    for (uint32_t id = from + blockIdx.x * blockDim.x + threadIdx.x; id < to; id += gridDim.x * blockDim.x) {
+        ClauseRecord &r = rec[id];
+        r.hist = 0;
+        r.total = 0;
+        r.last = -1;
+        r.birth = now;
+    }
+}
+
+// Training log of pass `fold` (before its counts are folded in): a share
+// `rate` of the live clauses known before this step (a hash of (seed, fold,
+// id) picks them), as (features a prediction for pass `fold` would have used,
+// whether the clause reported in it) rows.
+__global__ void log_kernel(HistoryArgs h, LogArgs lg, const int64_t *__restrict__ offsets,
+                           const uint32_t *__restrict__ orig, const uint32_t *__restrict__ alive, uint32_t n) {
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        if (alive != nullptr && !((alive[r >> 5] >> (r & 31)) & 1u)) continue;
+        const uint32_t id = orig[r];
+        if (id >= h.known_ids || id >= h.n_ids || !(unit_hash(lg.seed, (uint64_t) h.fold, id) < lg.rate)) continue;
+        const ClauseRecord &rec = h.rec[id];
+        if (!(rec.birth < h.fold)) continue;
+        const uint32_t c = h.slot ? rec.cur1 : rec.cur0;
+        float xl[kF];
+        clause_features((uint32_t) (offsets[r + 1] - offsets[r]), rec.lbd, h.fold - rec.birth,
+                        hist_at(rec.hist, rec.last, h.fold - 1), rec.total, rec.last < 0 ? -1 : h.fold - rec.last, xl);
+        const unsigned long long slot = atomicAdd(lg.count, 1ull) % lg.cap;
+#pragma unroll
+        for (int k = 0; k < kF; k++) lg.x[slot * kF + k] = xl[k];
+        lg.y[slot] = c ? 1.0f : 0.0f;
+    }
+}
+
+// Folds the counts of pass `fold` (slot h.slot) into the histories of the
+// clauses that pass reported and clears the counters for the pass two later.
+// A thread per id, in id order: the counters are read as one coalesced sweep
+// over the records, and only the reported clauses' records are written.
+__global__ void fold_kernel(HistoryArgs h, uint32_t n) {
+    for (uint32_t id = blockIdx.x * blockDim.x + threadIdx.x; id < n; id += gridDim.x * blockDim.x) {
+        ClauseRecord &r = h.rec[id];
+        const uint32_t c = h.slot ? r.cur1 : r.cur0;
+        if (c == 0) continue;
+        if (h.slot)
+            r.cur1 = 0;
+        else
+            r.cur0 = 0;
+        r.hist = hist_at(r.hist, r.last, h.fold) | (uint64_t) (c < 255u ? c : 255u);
+        r.total += c;
+        r.last = h.fold;
     }
 }
 
@@ -777,16 +821,20 @@ __global__ void __launch_bounds__(kSortThreads) bucket_scatter_kernel(const uint
     }
 }
 
+// Per report record of the pass: its slot count goes to its clause's counter
+// for the pass. The partitions' records are spread over all the blocks (a
+// block takes a stripe of one partition).
 __global__ void history_kernel(const gss_report *__restrict__ reports, const uint32_t *__restrict__ counts,
                                uint32_t n_parts, uint32_t cap_per_part, ClauseRecord *__restrict__ rec,
                                uint32_t n_ids, uint32_t slot) {
-    for (uint32_t q = blockIdx.x; q < n_parts; q += gridDim.x) {
-        const uint32_t m = min(counts[q], cap_per_part);
-        const gss_report *r = reports + (size_t) q * cap_per_part;
-        for (uint32_t i = threadIdx.x; i < m; i += blockDim.x) {
-            const uint32_t id = r[i].clause;
-            if (id < n_ids) atomicAdd(slot ? &rec[id].cur1 : &rec[id].cur0, (uint32_t) __popc(r[i].mask));
-        }
+    const uint32_t stripes = max(gridDim.x / n_parts, 1u);
+    const uint32_t q = blockIdx.x % n_parts, stripe = blockIdx.x / n_parts;
+    if (stripe >= stripes) return;
+    const uint32_t m = min(counts[q], cap_per_part);
+    const gss_report *r = reports + (size_t) q * cap_per_part;
+    for (uint32_t i = stripe * blockDim.x + threadIdx.x; i < m; i += stripes * blockDim.x) {
+        const uint32_t id = r[i].clause;
+        if (id < n_ids) atomicAdd(slot ? &rec[id].cur1 : &rec[id].cur0, (uint32_t) __popc(r[i].mask));
     }
 }
 
@@ -930,12 +978,17 @@ uint32_t head_cut(const OrderState &o, uint32_t n) {
 
 // Enqueues on `st` the scoring and ordering of pass q over the database as it
 // is now, into perm[q & 1]; returns the positions covered.
-int score_pass(gss_engine *eng, cudaStream_t st, int64_t q, uint32_t *covered) {
+int score_pass(gss_engine *eng, cudaStream_t st, int64_t q, uint32_t *covered, int *buf) {
     OrderState &o = *eng->order;
     const uint32_t n = (uint32_t) eng->n_clauses;
     const int64_t n_ids = eng->next_id;
     GSS_TRY(ensure_ids(eng, std::max<int64_t>(n_ids, 1)));
-    GSS_TRY(scorer_frags(&o.scorer, st));
+    // Between rescorings the last permutation serves (positions appended
+    // since it was built are scanned in place after it); a new layout, or
+    // every rescore_interval-th pass, scores and sorts again.
+    const int R = o.prm.rescore_interval;
+    const bool rescore = R <= 1 || q % R == 0 || !o.perm_valid || o.perm_layout != eng->layout_epoch || o.perm_n > n;
+    if (rescore) GSS_TRY(scorer_frags(&o.scorer, st));
     GSS_CUDA_TRY(cudaEventRecord(o.ev[0], st));
     HistoryArgs h = history_args(eng, (int32_t) (q - 1));
     // a pass's counts are folded once, by the first scoring of pass q
@@ -950,7 +1003,41 @@ int score_pass(gss_engine *eng, cudaStream_t st, int64_t q, uint32_t *covered) {
     lg.rate = (float) std::min(1.0, o.prm.log_rate > 0 ? o.prm.log_rate
                                                         : 2000.0 / (double) std::max<int64_t>(n_ids, 1));
     lg.seed = o.prm.seed;
-    DevBuf &perm = o.perm[q & 1];
+    // The history step of every pass: births of the ids first seen, the
+    // training rows of pass q-2, and the fold of its counts (only the clauses
+    // it reported are touched).
+    if (n_ids > o.known_ids) {
+        const uint32_t from = (uint32_t) o.known_ids, to = (uint32_t) n_ids;
+        birth_kernel<<<grid_for_n(to - from, eng->sm_count, 256), 256, 0, st>>>((ClauseRecord *) o.rec.ptr, from, to,
+                                                                               h.now);
+        GSS_CUDA_TRY(cudaGetLastError());
+    }
+    const uint32_t *alive = eng->n_dead > 0 ? (const uint32_t *) eng->alive.ptr : nullptr;
+    if (h.fold >= 0) {
+        if (lg.cap && n) {
+            log_kernel<<<grid_for_n(n, eng->sm_count, 256), 256, 0, st>>>(h, lg, (const int64_t *) eng->offsets.ptr,
+                                                                         (const uint32_t *) eng->orig.ptr, alive, n);
+            GSS_CUDA_TRY(cudaGetLastError());
+        }
+        // the ids known before this step (a newer id cannot have reported in pass q-2)
+        const uint32_t n_fold = (uint32_t) std::min<int64_t>(o.known_ids, o.cap_ids);
+        if (n_fold) {
+            fold_kernel<<<grid_for_n(n_fold, eng->sm_count, 256), 256, 0, st>>>(h, n_fold);
+            GSS_CUDA_TRY(cudaGetLastError());
+        }
+    }
+    o.known_ids = n_ids;
+    h.known_ids = (uint32_t) n_ids;
+    if (!rescore) {
+        // the permutation in force serves this pass
+        GSS_CUDA_TRY(cudaEventRecord(o.ev[1], st));
+        *covered = o.perm_n;
+        *buf = o.perm_buf;
+        return GSS_OK;
+    }
+    // the new permutation goes to the buffer the pass in flight is not reading
+    const int b = 1 - o.inflight_buf;
+    DevBuf &perm = o.perm[b];
     const uint32_t n_tiles = (uint32_t) (((size_t) n + kSortTile - 1) / kSortTile);
     GSS_TRY(perm.reserve(std::max<size_t>(n, 1) * sizeof(uint32_t)));
     GSS_TRY(o.bucket.reserve(std::max<size_t>(n, 1)));
@@ -958,11 +1045,10 @@ int score_pass(gss_engine *eng, cudaStream_t st, int64_t q, uint32_t *covered) {
     GSS_TRY(o.totals.reserve(kBuckets * sizeof(uint32_t)));
     GSS_TRY(o.key_of.reserve(kBuckets));
     if (n) {
-        // history fold, training log, features, MLP, score bucket
+        // features, MLP, score bucket
         score_kernel<<<grid_for_n((uint64_t) (n + 31) / 32 * 32, eng->sm_count, kMlpThreads), kMlpThreads, 0, st>>>(
-            h, lg, (const float *) o.scorer.w.ptr, (const uint32_t *) o.scorer.frag.ptr,
-            (const int64_t *) eng->offsets.ptr, (const uint32_t *) eng->orig.ptr,
-            eng->n_dead > 0 ? (const uint32_t *) eng->alive.ptr : nullptr, n, (uint8_t *) o.bucket.ptr);
+            h, (const float *) o.scorer.w.ptr, (const uint32_t *) o.scorer.frag.ptr,
+            (const int64_t *) eng->offsets.ptr, (const uint32_t *) eng->orig.ptr, alive, n, (uint8_t *) o.bucket.ptr);
         GSS_CUDA_TRY(cudaGetLastError());
         // the clauses per score bucket, then the sort key of each bucket:
         // score order in the head, plain order in the tail
@@ -991,8 +1077,12 @@ int score_pass(gss_engine *eng, cudaStream_t st, int64_t q, uint32_t *covered) {
         GSS_CUDA_TRY(cudaGetLastError());
     }
     GSS_CUDA_TRY(cudaEventRecord(o.ev[1], st));
-    o.known_ids = n_ids;
+    o.perm_valid = true;
+    o.perm_buf = b;
+    o.perm_n = n;
+    o.perm_layout = eng->layout_epoch;
     *covered = n;
+    *buf = b;
     return GSS_OK;
 }
 
@@ -1015,16 +1105,19 @@ int order_prepare(gss_engine *eng, const uint32_t **perm, uint32_t *head, uint32
     GSS_TRY(train_finish(eng, false));
     if (o.prm.retrain_interval > 0 && q > 0 && q % o.prm.retrain_interval == 0) GSS_TRY(train_start(eng));
     uint32_t n_scored = 0;
+    int buf = 0;
     if (o.pre_ready && o.pre_pass == q && o.pre_layout == eng->layout_epoch) {
         n_scored = o.pre_n;  // computed while the previous pass ran
+        buf = o.pre_buf;
     } else {
-        GSS_TRY(score_pass(eng, st, q, &n_scored));
+        GSS_TRY(score_pass(eng, st, q, &n_scored, &buf));
     }
     o.pre_ready = false;
     o.pass = q + 1;
     o.head = head_cut(o, n_scored);
     o.scored_n = n_scored;
-    *perm = (const uint32_t *) o.perm[q & 1].ptr;
+    o.inflight_buf = buf;
+    *perm = (const uint32_t *) o.perm[buf].ptr;
     *head = o.head;
     *covered = n_scored;
     GSS_CUDA_TRY(cudaEventRecord(o.ev[5], st));
@@ -1046,7 +1139,8 @@ int order_after_pass(gss_engine *eng, const DevBuf &reports, const DevBuf &count
     OrderState &o = *eng->order;
     GSS_CUDA_TRY(cudaEventRecord(o.ev[3], eng->stream));
     const int64_t q = o.pass - 1;  // the pass just enqueued
-    history_kernel<<<eng->n_parts, 256, 0, eng->stream>>>((const gss_report *) reports.ptr,
+    const unsigned hist_blocks = eng->n_parts * (unsigned) std::max(1, (eng->sm_count * 4) / (int) eng->n_parts);
+    history_kernel<<<hist_blocks, 256, 0, eng->stream>>>((const gss_report *) reports.ptr,
                                                           (const uint32_t *) counts.ptr, eng->n_parts,
                                                           eng->cap_per_part, (ClauseRecord *) o.rec.ptr,
                                                           (uint32_t) std::min<int64_t>(eng->next_id, o.cap_ids),
@@ -1057,12 +1151,14 @@ int order_after_pass(gss_engine *eng, const DevBuf &reports, const DevBuf &count
     // done (overlap) or pass q is: it folds the counts of pass q-1 (complete)
     GSS_CUDA_TRY(cudaStreamWaitEvent(o.score_stream, o.prm.overlap ? o.ev[2] : o.ev[3], 0));
     uint32_t covered = 0;
-    GSS_TRY(score_pass(eng, o.score_stream, q + 1, &covered));
+    int buf = 0;
+    GSS_TRY(score_pass(eng, o.score_stream, q + 1, &covered, &buf));
     GSS_CUDA_TRY(cudaEventRecord(o.ev_score_done, o.score_stream));
     o.pre_in_flight = true;
     o.pre_ready = true;
     o.pre_pass = q + 1;
     o.pre_n = covered;
+    o.pre_buf = buf;
     o.pre_layout = eng->layout_epoch;
     return GSS_OK;
 }
@@ -1089,6 +1185,7 @@ void gss_order_params_default(gss_order_params *p) {
     p->log_rate = 0.0;
     p->seed = 1;
     p->overlap = 1;
+    p->rescore_interval = 1;
 }
 
 int gss_order_enable(gss_engine *eng, const gss_order_params *p) {
@@ -1097,7 +1194,8 @@ int gss_order_enable(gss_engine *eng, const gss_order_params *p) {
     gss_order_params_default(&prm);
     if (p) prm = *p;
     if (!(prm.head_fraction >= 0.0 && prm.head_fraction <= 1.0) || prm.retrain_interval < 0 || prm.batch < 1 ||
-        prm.log_capacity < 0 || prm.log_capacity > (int64_t) 1 << 31 || !(prm.learning_rate > 0.0f))
+        prm.log_capacity < 0 || prm.log_capacity > (int64_t) 1 << 31 || !(prm.learning_rate > 0.0f) ||
+        prm.rescore_interval < 1)
         return set_error(GSS_ERR_INVALID, "bad learned-order parameters");
     GSS_CUDA_TRY(cudaSetDevice(eng->device));
     if (eng->order) order_destroy(eng);
@@ -1246,7 +1344,7 @@ int gss_order_scan_ranks(gss_engine *eng, const uint32_t *ids, int64_t n, int64_
     const uint32_t covered = o.scored_n;
     std::vector<uint32_t> perm(covered);
     if (covered)
-        GSS_CUDA_TRY(cudaMemcpy(perm.data(), o.perm[(o.pass - 1) & 1].ptr, covered * sizeof(uint32_t),
+        GSS_CUDA_TRY(cudaMemcpy(perm.data(), o.perm[o.inflight_buf].ptr, covered * sizeof(uint32_t),
                                 cudaMemcpyDeviceToHost));
     std::vector<int64_t> rank_of_pos((size_t) eng->n_clauses, -1);
     for (uint32_t r = 0; r < covered; r++)
@@ -1330,11 +1428,13 @@ int gss_order_clause_features(gss_engine *eng, const uint32_t *ids, int64_t n, f
             int32_t lst = r.last;
             if (fold) {
                 const uint32_t c = (q & 1) ? r.cur1 : r.cur0;
-                hh = (hh << 8) | (uint64_t) std::min<uint32_t>(c, 255u);
-                tot += c;
-                if (c) lst = (int32_t) (q - 2);
+                if (c) {
+                    hh = hist_at(hh, lst, (int32_t) (q - 2)) | (uint64_t) std::min<uint32_t>(c, 255u);
+                    tot += c;
+                    lst = (int32_t) (q - 2);
+                }
             }
-            clause_features(len, r.lbd, now - r.birth, hh, tot, lst < 0 ? -1 : now - lst, f);
+            clause_features(len, r.lbd, now - r.birth, hist_at(hh, lst, now - 1), tot, lst < 0 ? -1 : now - lst, f);
         } else {
             clause_features(len, r.lbd, 0, 0, 0, -1, f);  // first scored in the next pass
         }

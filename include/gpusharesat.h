@@ -341,6 +341,10 @@ typedef struct gss_order_params {
     uint64_t seed;             /* weight initialisation and minibatch sampling */
     int overlap;               /* 1: the next pass is scored while this pass's tail runs (default);
                                   0: once this pass has ended */
+    int rescore_interval;      /* passes per scoring and sort (default 1: every pass). Between two, each
+                                  pass only folds its reports into the history (and logs training rows)
+                                  and scans in the last permutation; clauses appended since it was built
+                                  are scanned in place after it. */
 } gss_order_params;
 
 void gss_order_params_default(gss_order_params *p);

@@ -99,8 +99,9 @@ def _small_engine(order=True, **params):
     return eng, wl
 
 
-def test_ordered_pass_reports_equal_plain(lib):
-    eng, wl = _small_engine(head_fraction=0.1, retrain_interval=0)
+@pytest.mark.parametrize("rescore", [1, 3])
+def test_ordered_pass_reports_equal_plain(lib, rescore):
+    eng, wl = _small_engine(head_fraction=0.1, retrain_interval=0, rescore_interval=rescore)
     rng = np.random.default_rng(5)
     for p in range(4):
         start = rng.integers(0, 2 ** 32, size=wl.n_words, dtype=np.uint32)
@@ -157,8 +158,11 @@ def test_ordered_wide_and_persistent_passes_equal_oracle(lib, variant):
         eng.close()
 
 
-def test_order_features_follow_the_report_history(lib):
-    eng, wl = _small_engine(head_fraction=0.25, retrain_interval=0)
+@pytest.mark.parametrize("rescore", [1, 3])
+def test_order_features_follow_the_report_history(lib, rescore):
+    """Every pass folds its reports into the history, whether it rescores
+    (every `rescore` passes) or keeps the last permutation."""
+    eng, wl = _small_engine(head_fraction=0.25, retrain_interval=0, rescore_interval=rescore)
     n = wl.n_clauses
     lens = np.diff(wl.offsets)
     rng = np.random.default_rng(6)
@@ -187,6 +191,51 @@ def test_order_features_follow_the_report_history(lib):
     want = np.stack([h.features(int(i), int(lens[i]), lbd_of[int(i)], 10) for i in sample])
     assert np.allclose(got, want, rtol=1e-6, atol=1e-6)
     eng.close()
+
+
+def test_rescore_interval_with_churn_matches_oracle(lib):
+    """Rescoring every 3 passes while clauses are deleted and appended: each
+    pass (head plus tail) reports exactly the live clauses' oracle reports;
+    the clauses appended since the last scoring are scanned in place after
+    the permutation."""
+    import gpusharesat_gb300 as g
+    import oracle
+    from gpusharesat_gb300 import workloads as W
+    rng = np.random.default_rng(21)
+    base = W.make_scale(seed=21, n_vars=2 ** 12, n_clauses=20000, n_solvers=32)
+    live = {c: base.lits[base.offsets[c]:base.offsets[c + 1]].tolist() for c in range(base.n_clauses)}
+    eng = g.Engine(0)
+    try:
+        eng.set_db(base.lits, base.offsets)
+        eng.set_state(base.state, base.start, base.solver_of_word)
+        eng.set_capacity(1 << 21)
+        eng.order_enable(head_fraction=0.25, retrain_interval=0, rescore_interval=3)
+        next_id = base.n_clauses
+        for p in range(7):
+            gone = rng.choice(sorted(live), size=500, replace=False)
+            eng.delete(gone)
+            for i in gone:
+                del live[int(i)]
+            lits, offs = W.distinct_var_clauses(rng, W.lengths_small(rng, 500), base.n_vars)
+            eng.append_db(lits, offs, np.arange(next_id, next_id + 500, dtype=np.uint32))
+            for k in range(500):
+                live[next_id + k] = lits[offs[k]:offs[k + 1]].tolist()
+            next_id += 500
+            eng.launch()
+            head = eng.wait_head()
+            got = np.concatenate([head, eng.copy_tail()])
+            ids = sorted(live)
+            ref_l = np.concatenate([np.asarray(live[i], np.int32) for i in ids])
+            ref_o = np.zeros(len(ids) + 1, np.int64)
+            ref_o[1:] = np.cumsum([len(live[i]) for i in ids])
+            ref = oracle.check(ref_l, ref_o, base.state, base.start, n_threads=8)
+            ref_ids = np.asarray(ids, np.uint32)[ref["clause"]]
+            want = set(zip(ref_ids.tolist(), ref["word"].tolist(), ref["mask"].tolist()))
+            assert len(got) == len(ref), p
+            assert set(zip(got["clause"].tolist(), got["word"].tolist(), got["mask"].tolist())) == want, p
+        assert eng.order_stats()["passes"] == 7
+    finally:
+        eng.close()
 
 
 def test_trained_order_front_loads_reports(lib):
