@@ -18,11 +18,13 @@
 //      m16 tiles, and each lane writes its clause's score bucket
 //   3. bucket_hist_kernel, bucket_scan_kernel, head_key_kernel, then a
 //      stable one-digit radix sort of positions (bucket_hist, bucket_scan,
-//      bucket_base, bucket_scatter) by key: the score bucket for the clauses
-//      of the head (the best buckets up to head_fraction of the clauses), one
-//      key for the tail. The plain position order is sorted by length, so a
-//      head bucket stays in length order (lane groups of a warp keep clauses
-//      of one length), and the tail keeps the plain order and its locality
+//      bucket_base, bucket_scatter) by key: the octave of predicted
+//      probability for the clauses of the head (the best buckets up to
+//      head_fraction of the clauses), one key for the tail. Inside a key the
+//      plain database order holds (variable ranges, then length), so the
+//      head keeps much of its state-row locality (its reports are delivered
+//      at the end of the head launch, whatever its inner order), and the
+//      tail keeps the plain order and its locality
 // After the pass (order_after_pass): history_kernel adds each report's slot
 // count to its clause's counter for the pass, and the scoring of the next
 // pass is enqueued on a stream of its own, behind the head of this pass: it
@@ -730,12 +732,12 @@ __device__ uint32_t block_scan_inplace(uint32_t *__restrict__ a, uint32_t n) {
     return carry;
 }
 
-// The sort key of each score bucket for the final order: the bucket itself
-// while the clauses of better buckets number fewer than `cut` (the head,
-// ordered by score), kBuckets - 2 for the rest (the tail, which then keeps
-// the plain position order and its memory locality), kBuckets - 1 for
-// deleted clauses. totals holds the clause count of each bucket. One block
-// of kBuckets threads.
+// The sort key of each score bucket for the final order: the bucket's octave
+// of predicted probability while the clauses of better buckets number fewer
+// than `cut` (the head, by octave, in database order inside an octave),
+// kBuckets - 2 for the rest (the tail, which then keeps the plain position
+// order and its memory locality), kBuckets - 1 for deleted clauses. totals
+// holds the clause count of each bucket. One block of kBuckets threads.
 __global__ void head_key_kernel(const uint32_t *__restrict__ totals, uint32_t cut, uint8_t *__restrict__ key_of) {
     __shared__ uint32_t before[kBuckets];
     const int b = threadIdx.x;
@@ -750,7 +752,11 @@ __global__ void head_key_kernel(const uint32_t *__restrict__ totals, uint32_t cu
         }
     }
     __syncthreads();
-    key_of[b] = (uint8_t) (b == kBuckets - 1 ? kBuckets - 1 : before[b] < cut ? b : kBuckets - 2);
+    // head buckets by octave of the predicted probability: within an octave
+    // the head keeps the database order (its state-row locality); the head's
+    // reports are delivered when the whole head launch ends, so the order
+    // inside it does not delay them
+    key_of[b] = (uint8_t) (b == kBuckets - 1 ? kBuckets - 1 : before[b] < cut ? b / kBucketsPerOctave : kBuckets - 2);
 }
 
 // Block b: exclusive scan of bucket b's per-tile counts; totals[b] = its sum.
