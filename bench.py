@@ -121,7 +121,7 @@ def load_traffic():
     path = os.path.join(ROOT, "profiles", "check_wide_persist_kernel_plain_scale.md")
     if os.path.exists(path):
         with open(path) as f:
-            m = re.search(r"traffic_bytes_per_launch:\s*([0-9]+)", f.read())
+            m = re.search(r"traffic_bytes_per_launch\s*[|:]\s*([0-9]+)", f.read())
             if m:
                 return int(m.group(1))
     return None
