@@ -15,6 +15,8 @@ e2e:   the same metric through the C ABI call gss_check_passes_host_cells
        steps overlap the current step's check.
 latency: submit-to-report p50/p99/p999 through the GpuClauseSharer C ABI
        (the serving shape; see serving_leg).
+learned_order: the learned scan order against the plain single launch on
+       its own workload (see learned_leg).
 The inputs (about 0.6 GB) are larger than the 129 MB L2, so no flush is
 needed between steps.
 
@@ -67,6 +69,8 @@ def parse():
     p.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     p.add_argument("--serving-seconds", type=float, default=3.0,
                    help="measured seconds per rate of the serving leg (0: skip it)")
+    p.add_argument("--learned-passes", type=int, default=120,
+                   help="passes of the learned-order leg (0: skip it)")
     return p.parse_args()
 
 
@@ -229,6 +233,41 @@ def serving_leg(seconds):
             "workload": "2^21 variables, 16e6-clause budget, 2e5 clauses/s stream, 64 solvers, batches of 1-32, "
                         "0.05%% planted reports, %.0f s measured per rate after 1 s warm-up" % seconds,
             "rates": rows}
+
+
+def learned_leg(passes):
+    """The composed form against the plain single launch on the learned-order
+    workload (bench_configs.learned): 2^21 variables, 4e6 clauses plus a
+    stream of 500 a pass, 2048 slots, reports planted at latent per-clause
+    rates; the persistent kernel with the learned head (25% of the scan) and
+    tail, the history every pass, the order rebuilt every 4 passes, retrained
+    halfway. Reports recall in the first 10% of the scan, delivery latency on
+    the device clock, sustained checks/s of back-to-back passes, and whether
+    every compared pass reported exactly the plain scan's set."""
+    import contextlib
+    import io
+    from gpusharesat_gb300 import bench_configs
+    args = argparse.Namespace(clauses=4_000_000, passes=passes, retrain=max(1, passes // 2), head_fraction=0.25,
+                              compare_every=10, throughput_passes=20, rescore=4, overlap=1, stream_per_pass=500)
+    with contextlib.redirect_stdout(io.StringIO()):
+        r = bench_configs.learned(args)
+    return {
+        "workload": "2^21 variables, 4e6 clauses + 500 a pass, 2048 slots, latent report rates Beta(0.5, 20); "
+                    "%d passes, retrained after %d, order rebuilt every 4 passes, head 25%% of the scan" % (
+                        passes, args.retrain),
+        "recall_first_10pct": {"learned": r["recall_first_10pct_learned"], "plain": r["recall_first_10pct_plain"]},
+        "device_latency_ms": {"learned_p50": r["device_latency_p50_ms_learned"],
+                              "learned_p99": r["device_latency_p99_ms_learned"],
+                              "plain_p50": r["device_latency_p50_ms_plain"],
+                              "plain_p99": r["device_latency_p99_ms_plain"]},
+        "sustained_checks_per_s": {"learned": r["sustained_checks_per_s_learned"],
+                                   "plain_single_launch": r["sustained_checks_per_s_plain"]},
+        "sustained_ms_per_pass": {"learned": r["sustained_ms_per_pass_learned"],
+                                  "plain_single_launch": r["sustained_ms_per_pass_plain"],
+                                  "persistent_without_order": r["sustained_ms_per_pass_persistent_no_order"]},
+        "same_reports_every_compared_pass": r["same_reports_every_compared_pass"],
+        "compared_passes": r["compared_passes"],
+    }
 
 
 def cpu_parity(wl, gpu_reports, threads=None):
@@ -452,6 +491,8 @@ def run_gpu(args):
         }
         if args.serving_seconds > 0 and args.workload == "scale":
             line["latency"] = serving_leg(args.serving_seconds)
+        if args.learned_passes > 0 and args.workload == "scale":
+            line["learned_order"] = learned_leg(args.learned_passes)
         if not args.no_cpu_baseline:
             line["parity"] = cpu_parity(wl, sizing_reports)
             v, cores, sample = cpu_baseline(wl, args.cpu_seconds)
