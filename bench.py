@@ -17,6 +17,8 @@ latency: submit-to-report p50/p99/p999 through the GpuClauseSharer C ABI
        (the serving shape; see serving_leg).
 learned_order: the learned scan order against the plain single launch on
        its own workload (see learned_leg).
+batching: uneven batches with churn, the persistent and bucketed forms
+       against the plain single launch (see batching_leg).
 The inputs (about 0.6 GB) are larger than the 129 MB L2, so no flush is
 needed between steps.
 
@@ -71,6 +73,8 @@ def parse():
                    help="measured seconds per rate of the serving leg (0: skip it)")
     p.add_argument("--learned-passes", type=int, default=120,
                    help="passes of the learned-order leg (0: skip it)")
+    p.add_argument("--batching-passes", type=int, default=3,
+                   help="passes of the batching leg (0: skip it)")
     return p.parse_args()
 
 
@@ -267,6 +271,31 @@ def learned_leg(passes):
                                   "persistent_without_order": r["sustained_ms_per_pass_persistent_no_order"]},
         "same_reports_every_compared_pass": r["same_reports_every_compared_pass"],
         "compared_passes": r["compared_passes"],
+    }
+
+
+def batching_leg(passes):
+    """Uneven batches with churn (bench_configs.batching) at 2e6 clauses:
+    48 solvers with U[4,64] assignments each, 5% clause churn per pass; the
+    autotuned persistent kernel replayed as a captured graph and the bucketed
+    kernel against one launch of the plain grid-stride kernel for all
+    batches and against one launch per solver; report sets compared on the
+    first pass."""
+    import contextlib
+    import io
+    from gpusharesat_gb300 import bench_configs
+    args = argparse.Namespace(clauses=2_000_000, passes=passes)
+    with contextlib.redirect_stdout(io.StringIO()):
+        r = bench_configs.batching(args)
+    return {
+        "workload": "2^20 variables, 2e6 clauses (lengths 1 + Zipf(1.2), at most 256), 48 solvers x U[4,64] "
+                    "assignments, 5%% churn per pass, %d passes" % passes,
+        "checks_per_s": {"batched_persistent_graph": r["batched_checks_per_s"],
+                         "bucketed_length_plan": r["bucketed_checks_per_s"],
+                         "plain_single_launch": r["single_checks_per_s"],
+                         "one_launch_per_solver": r["per_solver_checks_per_s"]},
+        "autotuned_variant": r["autotuned_variant"],
+        "exact": r["exact"],
     }
 
 
@@ -493,6 +522,8 @@ def run_gpu(args):
             line["latency"] = serving_leg(args.serving_seconds)
         if args.learned_passes > 0 and args.workload == "scale":
             line["learned_order"] = learned_leg(args.learned_passes)
+        if args.batching_passes > 0 and args.workload == "scale":
+            line["batching"] = batching_leg(args.batching_passes)
         if not args.no_cpu_baseline:
             line["parity"] = cpu_parity(wl, sizing_reports)
             v, cores, sample = cpu_baseline(wl, args.cpu_seconds)
