@@ -518,16 +518,20 @@ def run_gpu(args):
             "gpu_launches": gpu_launches,
             "clocks": clocks,
         }
-        if args.serving_seconds > 0 and args.workload == "scale":
+        # the other configurations' legs measure one GPU: they run at N = 1
+        # (in a multi-GPU run they would hold every rank's GPU for minutes)
+        one_gpu = world == 1 and args.workload == "scale"
+        if args.serving_seconds > 0 and one_gpu:
             line["latency"] = serving_leg(args.serving_seconds)
-        if args.learned_passes > 0 and args.workload == "scale":
+        if args.learned_passes > 0 and one_gpu:
             line["learned_order"] = learned_leg(args.learned_passes)
-        if args.batching_passes > 0 and args.workload == "scale":
+        if args.batching_passes > 0 and one_gpu:
             line["batching"] = batching_leg(args.batching_passes)
         if not args.no_cpu_baseline:
             line["parity"] = cpu_parity(wl, sizing_reports)
-            v, cores, sample = cpu_baseline(wl, args.cpu_seconds)
-            line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+            if world == 1:  # the CPU baseline is timed at N = 1 only
+                v, cores, sample = cpu_baseline(wl, args.cpu_seconds)
+                line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
         print(json.dumps(line), flush=True)
     eng.close()
     if world > 1:
